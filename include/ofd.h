@@ -1,0 +1,126 @@
+/*
+ * ofd.h — C ABI of the GB300 device runtime for the opesci-fd elastic
+ * velocity-stress hot path (libofd.so).
+ *
+ * The reference has no device runtime: its generated program
+ * (opesci/templates/regular3d_tmpl.py:41-118, emitted sample
+ * benchmarks/test3d.cpp) allocates the nine fields, runs the OpenMP time loop
+ * inside extern "C" opesci_execute() and computes error norms inside
+ * opesci_convergence().  This header is the device-side replacement of that
+ * generated body: the CUDA program emitted by opesci/templates/cuda_tmpl.py
+ * keeps the reference's three entry points and implements them on top of the
+ * calls below, and the batching/serving drivers call them directly.
+ *
+ * Conventions
+ *  - every call returns 0 on success or a negative OFD_E* code; the message of
+ *    the last failure on the calling thread is returned by ofd_last_error();
+ *  - host arrays use the reference layout float[dim1][dim2][dim3] (z fastest,
+ *    margins included), the layout of one time level of the reference's
+ *    real_t[2][dim1][dim2][dim3] field arrays (regulargrid.py:466-496);
+ *  - field numbers follow the reference's OpesciGrid order, velocities then
+ *    stresses (staggeredgrid.py:69-71): U V W Txx Tyy Tzz Txy Tyz Txz;
+ *  - one CUDA stream per handle; calls on one handle are not re-entrant,
+ *    different handles are independent.
+ */
+#ifndef OFD_H
+#define OFD_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OFD_OK 0
+#define OFD_EINVAL (-1)    /* bad argument or unsupported configuration */
+#define OFD_ECUDA (-2)     /* a CUDA call failed */
+#define OFD_ENOMEM (-3)    /* device allocation failed */
+#define OFD_ESTATE (-4)    /* call not valid in the handle's current state */
+#define OFD_ETIMEOUT (-5)  /* a bounded device wait expired */
+
+enum ofd_field { OFD_U = 0, OFD_V, OFD_W, OFD_TXX, OFD_TYY, OFD_TZZ, OFD_TXY, OFD_TYZ, OFD_TXZ, OFD_NFIELDS };
+
+enum ofd_storage { OFD_F32 = 0, OFD_F16 = 1, OFD_BF16 = 2, OFD_F64 = 3 };
+
+/* free-surface algorithm per face (staggeredgrid.py:214-232) */
+enum ofd_face_bc { OFD_BC_NONE = 0, OFD_BC_LEVANDER = 1, OFD_BC_ROBERTSSON = 2 };
+
+typedef struct ofd_config {
+    int dim[3];            /* dim1, dim2, dim3 = interior points + 2*margin */
+    int space_order;       /* 2, 4, 6 or 8; margin = space_order/2 */
+    int storage;           /* enum ofd_storage; arithmetic is FP32 (FP64 for OFD_F64) */
+    int legacy_bc;         /* 1: omit the Levander normal-stress recompute (older generator) */
+    int free_surface[6];   /* enum ofd_face_bc for faces x-, x+, y-, y+, z-, z+ */
+    double spacing[3];     /* dx1, dx2, dx3 */
+    double dt;
+    double weights[4];     /* staggered first-derivative weights c_1..c_R (R = space_order/2) */
+    float field_scale[9];  /* stored = value * scale (16-bit storage; powers of two; 0 = 1) */
+    int kernel_variant;    /* 0 = best available, 1 = plain (one thread per column) */
+} ofd_config;
+
+typedef struct ofd_handle ofd_handle;
+
+/* Lifecycle.  ofd_create allocates two time levels of the nine fields and the
+ * eight effective-media arrays on the current device, all zero. */
+int ofd_create(const ofd_config *cfg, ofd_handle **out);
+int ofd_destroy(ofd_handle *h);
+const char *ofd_last_error(void);
+/* bytes ofd_create would allocate for cfg (fields + media), for admission control */
+int ofd_footprint(const ofd_config *cfg, size_t *bytes);
+
+/* Media.  Constant media as the reference prints them (beta, lambda, mu;
+ * staggeredgrid.py:278-282), or raw rho/vp/vs arrays in the reference layout
+ * (the arrays opesci_read_simple_binary_ptr fills, src/opesciIO.cpp:319-342)
+ * from which beta, lambda, mu and the averaged beta1..3, mu12, mu13, mu23 of
+ * staggeredgrid.py:571-597 are computed on the device. */
+int ofd_set_media_const(ofd_handle *h, float beta, float lambda, float mu);
+int ofd_set_media(ofd_handle *h, const float *rho, const float *vp, const float *vs);
+
+/* Field transfer, reference layout, host memory (pageable or pinned). */
+int ofd_upload_field(ofd_handle *h, int field, int level, const float *host);
+int ofd_download_field(ofd_handle *h, int field, int level, float *host);
+/* Same with device memory in the reference layout. */
+int ofd_upload_field_device(ofd_handle *h, int field, int level, const float *dev);
+int ofd_download_field_device(ofd_handle *h, int field, int level, float *dev);
+int ofd_zero_fields(ofd_handle *h);
+
+/* Point source: after every step, T_ii[src] -= wavelet[step]/3 for the three
+ * normal stresses while step < nt (tests/src/test_ref_iso_elastic.cpp:274-290).
+ * (sx, sy, sz) is an array index including margins. */
+int ofd_set_source(ofd_handle *h, int sx, int sy, int sz, const float *wavelet, int nt);
+
+/* Ghost cells of one level as the reference's initialise_bc does for the
+ * initial level (staggeredgrid.py:866-879): stress mirrors, then velocity
+ * ghosts. */
+int ofd_apply_boundary_init(ofd_handle *h, int level);
+
+/* Advance nsteps time steps (staggered3d_tmpl.py:40-58 loop body): stress
+ * sweep, stress ghosts, velocity sweep, velocity ghosts, source.  Asynchronous
+ * on the handle's stream. */
+int ofd_step(ofd_handle *h, int nsteps);
+int ofd_sync(ofd_handle *h);
+/* completed steps; the newest level is steps % 2 */
+int ofd_get_step(ofd_handle *h, long *steps);
+int ofd_set_step(ofd_handle *h, long steps);
+
+/* FP64 sum of squares of each field over the interior [m, dim-m)^3 of a level. */
+int ofd_field_sumsq(ofd_handle *h, int level, double out[9]);
+
+/* Stream of the handle (cudaStream_t) for callers that interleave work. */
+void *ofd_stream(ofd_handle *h);
+
+/* Device pointer + layout of one field level:  element (x, y, z) of the level
+ * is at base[(x*dim2 + y)*pitch + z] in units of the storage type. */
+typedef struct ofd_field_view {
+    void *base;
+    long pitch;      /* elements between consecutive y rows */
+    int storage;
+    float scale;
+} ofd_field_view;
+int ofd_field_view_get(ofd_handle *h, int field, int level, ofd_field_view *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OFD_H */

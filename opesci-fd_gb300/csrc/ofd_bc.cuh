@@ -1,0 +1,220 @@
+// Free-surface ghost cells (stress and velocity), restating the ghost
+// equations of fields.py:192-381 and the loop ranges/order of
+// staggeredgrid.py:754-864.
+//
+// Phases.  The reference updates ghosts field by field, face normal by face
+// normal (x, then y, then z), and later faces read values written by earlier
+// ones (corners, and the Levander recompute overwriting planes a mirror has
+// read).  One launch per face normal d reproduces that: within a phase the
+// fields and the two sides are independent.  Velocity ghosts need two
+// launches per normal: the component along d first (staggeredgrid.py:829-832),
+// then the two tangential components that read it.
+//
+// Stress, face normal d, plane index b (lower b = m, upper b = n-m-1):
+//  * normal stress T_dd (unstaggered along d): T[b] = 0, T[b-+k] = -T[b+-k],
+//    k = 1..R-1; in-plane range [0, n) (fields.py:361-381);
+//  * shear stress with d among its indices (staggered along d):
+//    lower T[b-1-k] = -T[b+k], upper T[b+k] = -T[b-1-k], k = 0..R-1;
+//  * Levander, normal stress T_aa with a != d, plane b, in-plane range
+//    [m+1, n-m-1): T_aa(t1) = T_aa(t0) + dt (K1 D4_a v_a + K2 D4_e v_e) with
+//    K1 = lam+2mu - lam^2/(lam+2mu), K2 = lam - lam^2/(lam+2mu): the rate of
+//    T_aa with dv_d/dx_d eliminated through T_dd = 0 (fields.py:313-353).
+// Velocity, face normal d, in-plane range [1, n-1):
+//  * Levander, component along d (zero normal traction, 2nd-order FD):
+//    lower v_d[b-1] = v_d[b] + r sum_j (h_d/h_j)(v_j[b; j] - v_j[b; j-1]),
+//    upper v_d[b]   = v_d[b-1] - r sum_j (h_d/h_j)(v_j[b; j] - v_j[b; j-1]),
+//    r = lam/(lam+2mu) at plane b (fields.py:220-224);
+//  * Levander, tangential v_j (continuity of dT_jd/dt across the surface,
+//    fields.py:225-230), with G(p) = h_d (v_d[p; j+1] - v_d[p; j]) / h_j and
+//    mu_lo, mu_hi the effective shear modulus of T_jd at planes b-1, b:
+//    lower v_j[b-1] = v_j[b] + G(b-1) - (mu_hi/mu_lo)(v_j[b+1] - v_j[b] + G(b)),
+//    upper v_j[b+1] = v_j[b] - G(b) + (mu_lo/mu_hi)(v_j[b] - v_j[b-1] + G(b-1));
+//  * Robertsson: R ghost layers set to zero (fields.py:243-259).
+#pragma once
+#include "ofd_common.cuh"
+
+namespace ofd {
+
+__device__ __forceinline__ void plane_axes(int d, int &a1, int &a2) {
+  // a2 is the faster-varying in-plane axis (mapped to threadIdx.x)
+  if (d == 0) { a1 = 1; a2 = 2; }
+  else if (d == 1) { a1 = 0; a2 = 2; }
+  else { a1 = 0; a2 = 1; }
+}
+
+__device__ __forceinline__ long lin(const Geom &g, int x, int y, int z) {
+  return (long)x * g.plane + (long)y * g.P + z;
+}
+
+__device__ __forceinline__ int gdim(const Geom &g, int a) { return a == 0 ? g.n1 : (a == 1 ? g.n2 : g.n3); }
+
+// stride of axis a in elements
+__device__ __forceinline__ long gstride(const Geom &g, int a) { return a == 0 ? g.plane : (a == 1 ? g.P : 1); }
+
+__device__ __forceinline__ int mu_pair(int a, int b) {
+  const int lo = a < b ? a : b, hi = a < b ? b : a;
+  if (lo == 0 && hi == 1) return M_MU12;
+  if (lo == 0 && hi == 2) return M_MU13;
+  return M_MU23;
+}
+
+// Stress ghosts of face normal a.d: blockIdx.z = field(0..5)*2 + side.
+template <int R, typename S>
+__global__ void __launch_bounds__(256) stress_bc_kernel(BcArgs<S> a) {
+  typedef typename Storage<S>::C C;
+  const Geom g = a.g;
+  const int d = a.d;
+  int a1, a2;
+  plane_axes(d, a1, a2);
+  const int i2 = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i1 = blockIdx.y * blockDim.y + threadIdx.y;
+  const int fi = blockIdx.z >> 1, side = blockIdx.z & 1;
+  const int n1 = gdim(g, a1), n2 = gdim(g, a2), nd = gdim(g, d);
+  if (i1 >= n1 || i2 >= n2) return;
+  const int fb = a.face[2 * d + side];
+  if (fb == 0) return;
+  const int F = F_TXX + fi;
+  // directions of the stress component
+  const int dA = (fi < 3) ? fi : (fi == 3 ? 0 : (fi == 4 ? 1 : 0));
+  const int dB = (fi < 3) ? fi : (fi == 3 ? 1 : 2);
+  const bool normal = fi < 3;
+  const int m = g.m;
+  const int b = side == 0 ? m : nd - m - 1;
+  int c[3];
+  c[a1] = i1; c[a2] = i2; c[d] = 0;
+  const long base = lin(g, c[0], c[1], c[2]);
+  const long sd = gstride(g, d);
+  S *T = a.f1[F];
+  if (d == dA || d == dB) {
+    if (normal) {
+      T[base + b * sd] = Storage<S>::store(C(0), a.sc[F]);
+      const int sgn = side == 0 ? -1 : 1;
+#pragma unroll
+      for (int k = 1; k < R; ++k) {
+        const C v = Storage<S>::load(T[base + (b - sgn * k) * sd], a.inv[F]);
+        T[base + (b + sgn * k) * sd] = Storage<S>::store(-v, a.sc[F]);
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < R; ++k) {
+        const int dst = side == 0 ? b - 1 - k : b + k;
+        const int src = side == 0 ? b + k : b - 1 - k;
+        const C v = Storage<S>::load(T[base + src * sd], a.inv[F]);
+        T[base + dst * sd] = Storage<S>::store(-v, a.sc[F]);
+      }
+    }
+    return;
+  }
+  if (!normal || fb != 1 || !a.recompute) return;
+  if (i1 < m + 1 || i1 >= n1 - m - 1 || i2 < m + 1 || i2 >= n2 - m - 1) return;
+  // Levander recompute of T_aa (a = dA) on plane b
+  const int ax = dA;
+  const int e = 3 - ax - d;
+  const long o = base + b * sd;
+  const C lam = (C)a.media[M_LAM][o], mu = (C)a.media[M_MU][o];
+  const C l2m = lam + C(2) * mu;
+  const C q = lam * lam / l2m;
+  const C K1 = l2m - q, K2 = lam - q;
+  const long sa = gstride(g, ax), se = gstride(g, e);
+  const S *va = a.f0[F_U + ax], *ve = a.f0[F_U + e];
+  auto LV = [&](const S *p, int f, long off) -> C { return Storage<S>::load(p[o + off], a.inv[f]); };
+  const C Da = (a.c4[0] * (LV(va, F_U + ax, 0) - LV(va, F_U + ax, -sa)) +
+                a.c4[1] * (LV(va, F_U + ax, sa) - LV(va, F_U + ax, -2 * sa))) / a.h[ax];
+  const C De = (a.c4[0] * (LV(ve, F_U + e, 0) - LV(ve, F_U + e, -se)) +
+                a.c4[1] * (LV(ve, F_U + e, se) - LV(ve, F_U + e, -2 * se))) / a.h[e];
+  const C t0 = Storage<S>::load(a.f0[F][o], a.inv[F]);
+  T[o] = Storage<S>::store(t0 + a.dt * (K1 * Da + K2 * De), a.sc[F]);
+}
+
+// Velocity ghosts of face normal a.d.  sub 0: blockIdx.z = side (component
+// along d); sub 1: blockIdx.z = which tangential component (0/1)*2 + side.
+template <int R, typename S>
+__global__ void __launch_bounds__(256) velocity_bc_kernel(BcArgs<S> a) {
+  typedef typename Storage<S>::C C;
+  const Geom g = a.g;
+  const int d = a.d;
+  int a1, a2;
+  plane_axes(d, a1, a2);
+  const int i2 = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i1 = blockIdx.y * blockDim.y + threadIdx.y;
+  const int n1 = gdim(g, a1), n2 = gdim(g, a2), nd = gdim(g, d);
+  if (i1 < 1 || i1 >= n1 - 1 || i2 < 1 || i2 >= n2 - 1) return;
+  const int side = blockIdx.z & 1;
+  const int fb = a.face[2 * d + side];
+  if (fb == 0) return;
+  const int m = g.m;
+  const int b = side == 0 ? m : nd - m - 1;
+  int c[3];
+  c[a1] = i1; c[a2] = i2; c[d] = 0;
+  const long base = lin(g, c[0], c[1], c[2]);
+  const long sd = gstride(g, d);
+  const int comp = (a.sub == 0) ? d : ((blockIdx.z >> 1) == 0 ? a1 : a2);
+  const int F = F_U + comp;
+  S *v = a.f1[F];
+  if (fb == 2) {  // Robertsson
+    const bool stag = (comp == d);
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+      int idx;
+      if (stag) idx = side == 0 ? b - 1 - k : b + k;
+      else idx = side == 0 ? b - 1 - k : b + 1 + k;
+      v[base + idx * sd] = Storage<S>::store(C(0), a.sc[F]);
+    }
+    return;
+  }
+  auto LD = [&](int f, long off) -> C { return Storage<S>::load(a.f1[f][off], a.inv[f]); };
+  if (comp == d) {
+    const long ob = base + b * sd;
+    const C lam = (C)a.media[M_LAM][ob], mu = (C)a.media[M_MU][ob];
+    const C r = lam / (lam + C(2) * mu);
+    C s = 0;
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+      const int j = t == 0 ? a1 : a2;
+      const long sj = gstride(g, j);
+      s += (a.h[d] / a.h[j]) * (LD(F_U + j, ob) - LD(F_U + j, ob - sj));
+    }
+    if (side == 0)
+      v[base + (b - 1) * sd] = Storage<S>::store(LD(F, ob) + r * s, a.sc[F]);
+    else
+      v[ob] = Storage<S>::store(LD(F, ob - sd) - r * s, a.sc[F]);
+    return;
+  }
+  // tangential component v_j, j = comp
+  const int j = comp;
+  const long sj = gstride(g, j);
+  const int Fd = F_U + d;
+  const int mp = mu_pair(j, d);
+  const long ob = base + b * sd, obm = ob - sd;
+  const C mu_lo = (C)a.media[mp][obm], mu_hi = (C)a.media[mp][ob];
+  const C hr = a.h[d] / a.h[j];
+  const C Gm = hr * (LD(Fd, obm + sj) - LD(Fd, obm));   // G(b-1)
+  const C G0 = hr * (LD(Fd, ob + sj) - LD(Fd, ob));     // G(b)
+  if (side == 0) {
+    const C val = LD(F, ob) + Gm - (mu_hi / mu_lo) * (LD(F, ob + sd) - LD(F, ob) + G0);
+    v[obm] = Storage<S>::store(val, a.sc[F]);
+  } else {
+    const C val = LD(F, ob) - G0 + (mu_lo / mu_hi) * (LD(F, ob) - LD(F, obm) + Gm);
+    v[ob + sd] = Storage<S>::store(val, a.sc[F]);
+  }
+}
+
+template <typename S>
+__global__ void source_kernel(S *txx, S *tyy, S *tzz, long off, const float *w, int nt,
+                              const long *step, float s0, float s1, float s2) {
+  const long st = *step;
+  if (st < nt) {
+    const float v = w[st] / 3;
+    txx[off] = Storage<S>::store(Storage<S>::load(txx[off], 1.f / s0) - v, s0);
+    tyy[off] = Storage<S>::store(Storage<S>::load(tyy[off], 1.f / s1) - v, s1);
+    tzz[off] = Storage<S>::store(Storage<S>::load(tzz[off], 1.f / s2) - v, s2);
+  }
+}
+
+}  // namespace ofd
+
+namespace ofd {
+// Advances the device-side step counter read by source_kernel, so that a
+// captured step graph can be replayed without host-side arguments changing.
+static __global__ void step_tick(long *step) { *step += 1; }
+}  // namespace ofd

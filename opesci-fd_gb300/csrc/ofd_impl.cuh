@@ -1,0 +1,257 @@
+// Backend: the kernel launches of one (radius R, storage S) instantiation.
+// The runtime (ofd_runtime.cu) owns the handle and memory; each
+// ofd_inst_*.cu file instantiates Impl<R, S> for one storage type so the
+// variants compile in parallel.
+#pragma once
+#include "ofd_common.cuh"
+#include "ofd_sweep_plain.cuh"
+#include "ofd_sweep_tiled.cuh"
+#include "ofd_bc.cuh"
+
+namespace ofd {
+
+struct DevState {
+  Geom g;
+  int z0;
+  int storage;
+  size_t esize;
+  int R;
+  void *field[NF];     // field f, level 0, element (0,0,0) (z0 applied)
+  float *media[NM];    // media array, element (0,0,0) (z0 applied)
+  float scale[NF];
+  int face[6];
+  int legacy;
+  double dt, h[3], c[4];
+  long src_off;        // -1: no source
+  float *d_wav;
+  int nt;
+  int variant;         // 0 best, 1 plain
+  double *d_partial;   // reduction scratch (>= 2048 doubles)
+  long *d_step;        // device step counter (graph-safe source index)
+};
+
+struct Backend {
+  virtual ~Backend() {}
+  virtual void step(const DevState &s, int t0, cudaStream_t st) = 0;
+  virtual void boundary_init(const DevState &s, int level, cudaStream_t st) = 0;
+  virtual void to_padded(const DevState &s, const float *dense, int f, int level, cudaStream_t st) = 0;
+  virtual void from_padded(const DevState &s, float *dense, int f, int level, cudaStream_t st) = 0;
+  virtual void sumsq(const DevState &s, int level, double *d_out9, cudaStream_t st) = 0;
+};
+
+Backend *make_backend_f32(int R);
+Backend *make_backend_f64(int R);
+Backend *make_backend_f16(int R);
+Backend *make_backend_bf16(int R);
+
+// ---- generic kernels ------------------------------------------------------
+
+template <typename S>
+__global__ void dense_to_padded(const float *__restrict__ src, S *__restrict__ dst, Geom g, float sc) {
+  const long n = (long)g.n1 * g.n2 * g.n3;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const int z = (int)(i % g.n3);
+    const long r = i / g.n3;
+    const int y = (int)(r % g.n2);
+    const int x = (int)(r / g.n2);
+    dst[(long)x * g.plane + (long)y * g.P + z] = Storage<S>::store((typename Storage<S>::C)src[i], sc);
+  }
+}
+
+template <typename S>
+__global__ void padded_to_dense(const S *__restrict__ src, float *__restrict__ dst, Geom g, float inv) {
+  const long n = (long)g.n1 * g.n2 * g.n3;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const int z = (int)(i % g.n3);
+    const long r = i / g.n3;
+    const int y = (int)(r % g.n2);
+    const int x = (int)(r / g.n2);
+    dst[i] = (float)Storage<S>::load(src[(long)x * g.plane + (long)y * g.P + z], inv);
+  }
+}
+
+// Deterministic FP64 sum of squares over the interior of 9 fields: one block
+// row per field, fixed grid, tree reduction, then a single-block pass.
+template <typename S>
+__global__ void sumsq_partial(DevState s, int level, double *partial) {
+  const Geom g = s.g;
+  const int f = blockIdx.y;
+  const S *p = (const S *)s.field[f] + (long)level * g.level;
+  const long nx = g.n1 - 2 * g.m, ny = g.n2 - 2 * g.m, nz = g.n3 - 2 * g.m;
+  const long n = nx * ny * nz;
+  const float inv = 1.f / s.scale[f];
+  double acc = 0;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const int z = (int)(i % nz) + g.m;
+    const long r = i / nz;
+    const int y = (int)(r % ny) + g.m;
+    const int x = (int)(r / ny) + g.m;
+    const double v = (double)Storage<S>::load(p[(long)x * g.plane + (long)y * g.P + z], inv);
+    acc += v * v;
+  }
+  __shared__ double sh[256];
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[f * gridDim.x + blockIdx.x] = sh[0];
+}
+
+static __global__ void sumsq_final(const double *partial, int nblk, double *out) {
+  const int f = threadIdx.x;
+  if (f < NF) {
+    double a = 0;
+    for (int i = 0; i < nblk; ++i) a += partial[f * nblk + i];
+    out[f] = a;
+  }
+}
+
+// ---- Impl -----------------------------------------------------------------
+
+template <int R, typename S>
+struct Impl : Backend {
+  typedef typename Storage<S>::C C;
+
+  S *fp(const DevState &s, int f, int lvl) const { return (S *)s.field[f] + (long)lvl * s.g.level; }
+
+  SweepArgs<S> sweep_args(const DevState &s, int t0, bool stress) const {
+    SweepArgs<S> a;
+    a.g = s.g;
+    const int t1 = 1 - t0;
+    for (int f = 0; f < NF; ++f) {
+      const bool is_v = f < 3;
+      // stress sweep reads everything at t0; velocity sweep reads V(t0), T(t1)
+      const int lin = stress ? t0 : (is_v ? t0 : t1);
+      a.in[f] = fp(s, f, lin);
+      a.out[f] = fp(s, f, t1);
+      a.sc[f] = s.scale[f];
+      a.inv[f] = 1.f / s.scale[f];
+    }
+    for (int i = 0; i < NM; ++i) a.media[i] = s.media[i];
+    a.dt = (C)s.dt;
+    a.ih1 = (C)(1.0 / s.h[0]);
+    a.ih2 = (C)(1.0 / s.h[1]);
+    a.ih3 = (C)(1.0 / s.h[2]);
+    for (int k = 0; k < 4; ++k) a.c[k] = (C)s.c[k];
+    a.xchunk = 0;
+    return a;
+  }
+
+  BcArgs<S> bc_args(const DevState &s, int t1, int t0, int recompute) const {
+    BcArgs<S> a;
+    a.g = s.g;
+    for (int f = 0; f < NF; ++f) {
+      a.f1[f] = fp(s, f, t1);
+      a.f0[f] = fp(s, f, t0);
+      a.sc[f] = s.scale[f];
+      a.inv[f] = 1.f / s.scale[f];
+    }
+    for (int i = 0; i < NM; ++i) a.media[i] = s.media[i];
+    for (int i = 0; i < 6; ++i) a.face[i] = s.face[i];
+    a.recompute = recompute;
+    a.dt = (C)s.dt;
+    for (int i = 0; i < 3; ++i) a.h[i] = (C)s.h[i];
+    a.c4[0] = (C)(9.0 / 8.0);
+    a.c4[1] = (C)(-1.0 / 24.0);
+    a.d = 0;
+    a.sub = 0;
+    return a;
+  }
+
+  static dim3 face_grid(const Geom &g, int d, int z) {
+    int n1, n2;
+    if (d == 0) { n1 = g.n2; n2 = g.n3; }
+    else if (d == 1) { n1 = g.n1; n2 = g.n3; }
+    else { n1 = g.n1; n2 = g.n2; }
+    return dim3((n2 + 31) / 32, (n1 + 7) / 8, z);
+  }
+
+  void stress_bc(const DevState &s, int t1, int t0, int recompute, cudaStream_t st) {
+    BcArgs<S> a = bc_args(s, t1, t0, recompute);
+    for (int d = 0; d < 3; ++d) {
+      a.d = d;
+      stress_bc_kernel<R, S><<<face_grid(s.g, d, 12), dim3(32, 8), 0, st>>>(a);
+    }
+  }
+
+  void velocity_bc(const DevState &s, int t1, cudaStream_t st) {
+    BcArgs<S> a = bc_args(s, t1, t1, 0);
+    for (int d = 0; d < 3; ++d) {
+      a.d = d;
+      a.sub = 0;
+      velocity_bc_kernel<R, S><<<face_grid(s.g, d, 2), dim3(32, 8), 0, st>>>(a);
+      a.sub = 1;
+      velocity_bc_kernel<R, S><<<face_grid(s.g, d, 4), dim3(32, 8), 0, st>>>(a);
+    }
+  }
+
+  void sweeps(const DevState &s, int t0, bool stress, cudaStream_t st) {
+    SweepArgs<S> a = sweep_args(s, t0, stress);
+    const Geom &g = s.g;
+    const int nx = g.n1 - 2 * g.m, ny = g.n2 - 2 * g.m, nz = g.n3 - 2 * g.m;
+    if (s.variant != 1 && tiled_supported<R, S>(g)) {
+      if (stress) launch_stress_tiled<R, S>(a, st);
+      else launch_velocity_tiled<R, S>(a, st);
+      return;
+    }
+    // plain: aim for >= 4 waves of 152 SMs
+    dim3 blk(32, 8);
+    dim3 grd((nz + 31) / 32, (ny + 7) / 8, 1);
+    long ctas = (long)grd.x * grd.y;
+    int chunks = (int)((152L * 8 + ctas - 1) / ctas);
+    if (chunks < 1) chunks = 1;
+    if (chunks > nx) chunks = nx;
+    a.xchunk = (nx + chunks - 1) / chunks;
+    grd.z = (nx + a.xchunk - 1) / a.xchunk;
+    if (stress) stress_plain<R, S><<<grd, blk, 0, st>>>(a);
+    else velocity_plain<R, S><<<grd, blk, 0, st>>>(a);
+  }
+
+  void step(const DevState &s, int t0, cudaStream_t st) override {
+    const int t1 = 1 - t0;
+    sweeps(s, t0, true, st);
+    stress_bc(s, t1, t0, s.legacy ? 0 : 1, st);
+    sweeps(s, t0, false, st);
+    velocity_bc(s, t1, st);
+    if (s.src_off >= 0) {
+      source_kernel<S><<<1, 1, 0, st>>>(fp(s, F_TXX, t1), fp(s, F_TYY, t1), fp(s, F_TZZ, t1), s.src_off,
+                                        s.d_wav, s.nt, s.d_step, s.scale[F_TXX], s.scale[F_TYY],
+                                        s.scale[F_TZZ]);
+    }
+    step_tick<<<1, 1, 0, st>>>(s.d_step);
+  }
+
+  void boundary_init(const DevState &s, int level, cudaStream_t st) override {
+    stress_bc(s, level, level, 0, st);
+    velocity_bc(s, level, st);
+  }
+
+  void to_padded(const DevState &s, const float *dense, int f, int level, cudaStream_t st) override {
+    dense_to_padded<S><<<1216, 256, 0, st>>>(dense, fp(s, f, level), s.g, s.scale[f]);
+  }
+
+  void from_padded(const DevState &s, float *dense, int f, int level, cudaStream_t st) override {
+    padded_to_dense<S><<<1216, 256, 0, st>>>(fp(s, f, level), dense, s.g, 1.f / s.scale[f]);
+  }
+
+  void sumsq(const DevState &s, int level, double *d_out9, cudaStream_t st) override {
+    const int nblk = 128;
+    sumsq_partial<S><<<dim3(nblk, NF), 256, 0, st>>>(s, level, s.d_partial);
+    sumsq_final<<<1, 32, 0, st>>>(s.d_partial, nblk, d_out9);
+  }
+};
+
+template <typename S>
+Backend *make_backend_t(int R) {
+  switch (R) {
+    case 1: return new Impl<1, S>();
+    case 2: return new Impl<2, S>();
+    case 3: return new Impl<3, S>();
+    case 4: return new Impl<4, S>();
+  }
+  return nullptr;
+}
+
+}  // namespace ofd

@@ -1,0 +1,450 @@
+// Device runtime of the opesci-fd elastic hot path: handle lifecycle, HBM
+// layout, media preprocessing, transfers and the time loop, exported through
+// the C ABI of include/ofd.h.
+#include <cstdio>
+#include <cstring>
+#include <cstdarg>
+#include <string>
+#include <vector>
+
+#include "ofd.h"
+#include "ofd_impl.cuh"
+
+namespace ofd {
+
+static thread_local std::string g_last_error;
+
+static int fail(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+#define OFD_CUDA(call)                                                                   \
+  do {                                                                                   \
+    cudaError_t _e = (call);                                                             \
+    if (_e != cudaSuccess)                                                               \
+      return fail(OFD_ECUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(_e),     \
+                  __FILE__, __LINE__);                                                   \
+  } while (0)
+
+// Media preprocessing (staggeredgrid.py:571-597), evaluated in double and
+// rounded to float like the reference's C expressions, on the whole padded
+// grid with upper neighbours clamped at the last index.
+__global__ void media_base_kernel(const float *rho, const float *vp, const float *vs, float *beta,
+                                  float *lam, float *mu, long n) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const double r = rho[i], p = vp[i], s = vs[i];
+    beta[i] = (float)(1.0 / r);
+    lam[i] = (float)(r * (p * p - 2.0 * (s * s)));
+    mu[i] = (float)(r * (s * s));
+  }
+}
+
+__global__ void media_avg_kernel(const float *beta, const float *lam, const float *mu, Geom g,
+                                 float *o_lam, float *o_mu, float *o_mu12, float *o_mu13,
+                                 float *o_mu23, float *o_b1, float *o_b2, float *o_b3) {
+  const long n = (long)g.n1 * g.n2 * g.n3;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const int z = (int)(i % g.n3);
+    const long r = i / g.n3;
+    const int y = (int)(r % g.n2);
+    const int x = (int)(r / g.n2);
+    const int x1 = x + 1 < g.n1 ? x + 1 : x, y1 = y + 1 < g.n2 ? y + 1 : y, z1 = z + 1 < g.n3 ? z + 1 : z;
+    auto D = [&](int a, int b, int c) { return ((long)a * g.n2 + b) * g.n3 + c; };
+    const long o = (long)x * g.plane + (long)y * g.P + z;
+    o_lam[o] = lam[i];
+    o_mu[o] = mu[i];
+    const float b0 = beta[i];
+    o_b1[o] = (b0 + beta[D(x1, y, z)]) * 0.5f;
+    o_b2[o] = (b0 + beta[D(x, y1, z)]) * 0.5f;
+    o_b3[o] = (b0 + beta[D(x, y, z1)]) * 0.5f;
+    const double m0 = 1.0 / (double)mu[i];
+    o_mu12[o] = (float)(1.0 / (0.25 * (m0 + 1.0 / (double)mu[D(x1, y, z)] + 1.0 / (double)mu[D(x, y1, z)] +
+                                       1.0 / (double)mu[D(x1, y1, z)])));
+    o_mu13[o] = (float)(1.0 / (0.25 * (m0 + 1.0 / (double)mu[D(x1, y, z)] + 1.0 / (double)mu[D(x, y, z1)] +
+                                       1.0 / (double)mu[D(x1, y, z1)])));
+    o_mu23[o] = (float)(1.0 / (0.25 * (m0 + 1.0 / (double)mu[D(x, y1, z)] + 1.0 / (double)mu[D(x, y, z1)] +
+                                       1.0 / (double)mu[D(x, y1, z1)])));
+  }
+}
+
+__global__ void fill_kernel(float *p, long n, float v) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) p[i] = v;
+}
+
+}  // namespace ofd
+
+using namespace ofd;
+
+struct ofd_handle {
+  ofd_config cfg;
+  DevState s;
+  Backend *be = nullptr;
+  cudaStream_t stream = nullptr;
+  int device = 0;
+  void *fields_raw = nullptr;   // one allocation for all fields
+  void *media_raw = nullptr;    // one allocation for all media
+  size_t field_bytes = 0, media_bytes = 0;
+  long media_elems = 0;         // elements of one media array (padded)
+  long level_elems = 0;         // elements of one field level (padded)
+  long steps = 0;
+  double *d_out = nullptr;      // 16 doubles
+};
+
+namespace {
+
+struct Layout {
+  Geom g;
+  int z0;
+  size_t esize;
+  long field_elems;   // per field (2 levels), rounded for 256-B alignment
+  long media_elems;
+};
+
+size_t storage_size(int st) {
+  switch (st) {
+    case OFD_F32: return 4;
+    case OFD_F64: return 8;
+    case OFD_F16: case OFD_BF16: return 2;
+  }
+  return 0;
+}
+
+int check_config(const ofd_config *c) {
+  if (!c) return fail(OFD_EINVAL, "null config");
+  if (c->space_order != 2 && c->space_order != 4 && c->space_order != 6 && c->space_order != 8)
+    return fail(OFD_EINVAL, "space_order %d not supported (2, 4, 6, 8)", c->space_order);
+  if (storage_size(c->storage) == 0) return fail(OFD_EINVAL, "unknown storage %d", c->storage);
+  const int m = c->space_order / 2;
+  for (int i = 0; i < 3; ++i) {
+    if (c->dim[i] < 4 * m + 2) return fail(OFD_EINVAL, "dim%d = %d too small for space order %d", i + 1, c->dim[i], c->space_order);
+    if (c->dim[i] > (1 << 20)) return fail(OFD_EINVAL, "dim%d = %d too large", i + 1, c->dim[i]);
+    if (!(c->spacing[i] > 0)) return fail(OFD_EINVAL, "spacing %d must be > 0", i + 1);
+  }
+  if (!(c->dt > 0)) return fail(OFD_EINVAL, "dt must be > 0");
+  for (int i = 0; i < 6; ++i)
+    if (c->free_surface[i] < 0 || c->free_surface[i] > 2) return fail(OFD_EINVAL, "bad free_surface[%d]", i);
+  return OFD_OK;
+}
+
+Layout make_layout(const ofd_config *c) {
+  Layout L;
+  L.esize = storage_size(c->storage);
+  const int m = c->space_order / 2;
+  const int A = (int)(128 / L.esize);     // elements per 128 B
+  L.z0 = (A - (m % A)) % A;
+  const long P = ((long)(L.z0 + c->dim[2]) + A - 1) / A * A;
+  L.g.n1 = c->dim[0];
+  L.g.n2 = c->dim[1];
+  L.g.n3 = c->dim[2];
+  L.g.m = m;
+  L.g.P = P;
+  L.g.plane = (long)c->dim[1] * P;
+  const long lvl = (long)c->dim[0] * L.g.plane;
+  // keep every level / field base 256-B aligned
+  const long align_e = (long)(256 / L.esize);
+  L.g.level = (lvl + align_e - 1) / align_e * align_e;
+  L.field_elems = 2 * L.g.level;
+  // media are float; their own pitch must match field geometry, so they use
+  // the float layout with the same z0 rule
+  L.media_elems = 0;
+  return L;
+}
+
+Geom media_geom(const ofd_config *c, int *z0) {
+  ofd_config f = *c;
+  f.storage = OFD_F32;
+  Layout L = make_layout(&f);
+  *z0 = L.z0;
+  return L.g;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *ofd_last_error(void) { return g_last_error.c_str(); }
+
+int ofd_footprint(const ofd_config *cfg, size_t *bytes) {
+  int rc = check_config(cfg);
+  if (rc) return rc;
+  Layout L = make_layout(cfg);
+  int mz0;
+  Geom mg = media_geom(cfg, &mz0);
+  *bytes = (size_t)L.field_elems * L.esize * NF + (size_t)mg.level * sizeof(float) * NM + 4096;
+  return OFD_OK;
+}
+
+int ofd_create(const ofd_config *cfg, ofd_handle **out) {
+  if (!out) return fail(OFD_EINVAL, "null out");
+  *out = nullptr;
+  int rc = check_config(cfg);
+  if (rc) return rc;
+  ofd_handle *h = new ofd_handle();
+  h->cfg = *cfg;
+  Layout L = make_layout(cfg);
+  int mz0;
+  Geom mg = media_geom(cfg, &mz0);
+  // Media use the float layout; kernels index media with the field geometry,
+  // so the two must coincide element for element.  For 16-bit or 64-bit
+  // storage the field layout differs, so media are laid out with the field
+  // geometry (pitch/z0) but float elements.
+  h->s.g = L.g;
+  h->s.z0 = L.z0;
+  h->s.storage = cfg->storage;
+  h->s.esize = L.esize;
+  h->s.R = cfg->space_order / 2;
+  (void)mg;
+  h->level_elems = L.g.level;
+  h->field_bytes = (size_t)L.field_elems * L.esize;
+  h->media_elems = L.g.level;  // media share the field geometry
+  h->media_bytes = (size_t)h->media_elems * sizeof(float);
+  cudaGetDevice(&h->device);
+  cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) { delete h; return fail(OFD_ECUDA, "cudaStreamCreate: %s", cudaGetErrorString(e)); }
+  e = cudaMalloc(&h->fields_raw, h->field_bytes * NF);
+  if (e != cudaSuccess) {
+    cudaStreamDestroy(h->stream);
+    delete h;
+    cudaGetLastError();
+    return fail(OFD_ENOMEM, "cudaMalloc of %zu field bytes failed: %s", h->field_bytes * NF, cudaGetErrorString(e));
+  }
+  e = cudaMalloc(&h->media_raw, h->media_bytes * NM + 4 * 4096);
+  if (e != cudaSuccess) {
+    cudaFree(h->fields_raw);
+    cudaStreamDestroy(h->stream);
+    delete h;
+    cudaGetLastError();
+    return fail(OFD_ENOMEM, "cudaMalloc of %zu media bytes failed: %s", h->media_bytes * NM, cudaGetErrorString(e));
+  }
+  cudaMemsetAsync(h->fields_raw, 0, h->field_bytes * NF, h->stream);
+  cudaMemsetAsync(h->media_raw, 0, h->media_bytes * NM + 4 * 4096, h->stream);
+  char *fb = (char *)h->fields_raw;
+  for (int f = 0; f < NF; ++f) h->s.field[f] = fb + f * h->field_bytes + (size_t)L.z0 * L.esize;
+  char *mb = (char *)h->media_raw;
+  // media element (x,y,z) at the same linear offset as the field element
+  for (int i = 0; i < NM; ++i) h->s.media[i] = (float *)(mb + i * h->media_bytes) + L.z0;
+  char *extra = mb + NM * h->media_bytes;
+  h->s.d_partial = (double *)extra;                    // 2048 doubles = 16 KB? keep 1152 used
+  h->s.d_step = (long *)(extra + 2 * 4096 + 1024);
+  h->d_out = (double *)(extra + 2 * 4096 + 2048);
+  h->s.d_wav = nullptr;
+  h->s.src_off = -1;
+  h->s.nt = 0;
+  for (int f = 0; f < NF; ++f) h->s.scale[f] = cfg->field_scale[f] > 0 ? cfg->field_scale[f] : 1.f;
+  if (cfg->storage == OFD_F32 || cfg->storage == OFD_F64)
+    for (int f = 0; f < NF; ++f) h->s.scale[f] = 1.f;
+  for (int i = 0; i < 6; ++i) h->s.face[i] = cfg->free_surface[i];
+  h->s.legacy = cfg->legacy_bc;
+  h->s.dt = cfg->dt;
+  for (int i = 0; i < 3; ++i) h->s.h[i] = cfg->spacing[i];
+  for (int k = 0; k < 4; ++k) h->s.c[k] = cfg->weights[k];
+  h->s.variant = cfg->kernel_variant;
+  switch (cfg->storage) {
+    case OFD_F32: h->be = make_backend_f32(h->s.R); break;
+    case OFD_F64: h->be = make_backend_f64(h->s.R); break;
+    case OFD_F16: h->be = make_backend_f16(h->s.R); break;
+    case OFD_BF16: h->be = make_backend_bf16(h->s.R); break;
+  }
+  e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess || !h->be) {
+    int code = fail(OFD_ECUDA, "initialisation failed: %s", cudaGetErrorString(e));
+    ofd_destroy(h);
+    return code;
+  }
+  *out = h;
+  return OFD_OK;
+}
+
+int ofd_destroy(ofd_handle *h) {
+  if (!h) return OFD_OK;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  delete h->be;
+  if (h->s.d_wav) cudaFree(h->s.d_wav);
+  if (h->fields_raw) cudaFree(h->fields_raw);
+  if (h->media_raw) cudaFree(h->media_raw);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return OFD_OK;
+}
+
+void *ofd_stream(ofd_handle *h) { return h ? (void *)h->stream : nullptr; }
+
+int ofd_set_media_const(ofd_handle *h, float beta, float lambda, float mu) {
+  if (!h) return fail(OFD_EINVAL, "null handle");
+  const long n = h->media_elems;
+  const float vals[NM] = {lambda, mu, mu, mu, mu, beta, beta, beta};
+  for (int i = 0; i < NM; ++i)
+    fill_kernel<<<1216, 256, 0, h->stream>>>(h->s.media[i] - h->s.z0, n, vals[i]);
+  OFD_CUDA(cudaGetLastError());
+  OFD_CUDA(cudaStreamSynchronize(h->stream));
+  return OFD_OK;
+}
+
+int ofd_set_media(ofd_handle *h, const float *rho, const float *vp, const float *vs) {
+  if (!h || !rho || !vp || !vs) return fail(OFD_EINVAL, "null argument");
+  const Geom &g = h->s.g;
+  const long n = (long)g.n1 * g.n2 * g.n3;
+  float *tmp = nullptr;
+  OFD_CUDA(cudaMallocAsync((void **)&tmp, sizeof(float) * n * 6, h->stream));
+  OFD_CUDA(cudaMemcpyAsync(tmp, rho, sizeof(float) * n, cudaMemcpyHostToDevice, h->stream));
+  OFD_CUDA(cudaMemcpyAsync(tmp + n, vp, sizeof(float) * n, cudaMemcpyHostToDevice, h->stream));
+  OFD_CUDA(cudaMemcpyAsync(tmp + 2 * n, vs, sizeof(float) * n, cudaMemcpyHostToDevice, h->stream));
+  media_base_kernel<<<1216, 256, 0, h->stream>>>(tmp, tmp + n, tmp + 2 * n, tmp + 3 * n, tmp + 4 * n, tmp + 5 * n, n);
+  media_avg_kernel<<<1216, 256, 0, h->stream>>>(tmp + 3 * n, tmp + 4 * n, tmp + 5 * n, g, h->s.media[M_LAM],
+                                                h->s.media[M_MU], h->s.media[M_MU12], h->s.media[M_MU13],
+                                                h->s.media[M_MU23], h->s.media[M_B1], h->s.media[M_B2],
+                                                h->s.media[M_B3]);
+  OFD_CUDA(cudaGetLastError());
+  OFD_CUDA(cudaFreeAsync(tmp, h->stream));
+  OFD_CUDA(cudaStreamSynchronize(h->stream));
+  return OFD_OK;
+}
+
+static int check_fl(ofd_handle *h, int field, int level) {
+  if (!h) return fail(OFD_EINVAL, "null handle");
+  if (field < 0 || field >= NF) return fail(OFD_EINVAL, "bad field %d", field);
+  if (level < 0 || level > 1) return fail(OFD_EINVAL, "bad level %d", level);
+  return OFD_OK;
+}
+
+int ofd_upload_field_device(ofd_handle *h, int field, int level, const float *dev) {
+  int rc = check_fl(h, field, level);
+  if (rc) return rc;
+  h->be->to_padded(h->s, dev, field, level, h->stream);
+  OFD_CUDA(cudaGetLastError());
+  return OFD_OK;
+}
+
+int ofd_download_field_device(ofd_handle *h, int field, int level, float *dev) {
+  int rc = check_fl(h, field, level);
+  if (rc) return rc;
+  h->be->from_padded(h->s, dev, field, level, h->stream);
+  OFD_CUDA(cudaGetLastError());
+  return OFD_OK;
+}
+
+int ofd_upload_field(ofd_handle *h, int field, int level, const float *host) {
+  int rc = check_fl(h, field, level);
+  if (rc) return rc;
+  const Geom &g = h->s.g;
+  const long n = (long)g.n1 * g.n2 * g.n3;
+  float *tmp = nullptr;
+  OFD_CUDA(cudaMallocAsync((void **)&tmp, sizeof(float) * n, h->stream));
+  OFD_CUDA(cudaMemcpyAsync(tmp, host, sizeof(float) * n, cudaMemcpyHostToDevice, h->stream));
+  h->be->to_padded(h->s, tmp, field, level, h->stream);
+  OFD_CUDA(cudaGetLastError());
+  OFD_CUDA(cudaFreeAsync(tmp, h->stream));
+  OFD_CUDA(cudaStreamSynchronize(h->stream));
+  return OFD_OK;
+}
+
+int ofd_download_field(ofd_handle *h, int field, int level, float *host) {
+  int rc = check_fl(h, field, level);
+  if (rc) return rc;
+  const Geom &g = h->s.g;
+  const long n = (long)g.n1 * g.n2 * g.n3;
+  float *tmp = nullptr;
+  OFD_CUDA(cudaMallocAsync((void **)&tmp, sizeof(float) * n, h->stream));
+  h->be->from_padded(h->s, tmp, field, level, h->stream);
+  OFD_CUDA(cudaGetLastError());
+  OFD_CUDA(cudaMemcpyAsync(host, tmp, sizeof(float) * n, cudaMemcpyDeviceToHost, h->stream));
+  OFD_CUDA(cudaFreeAsync(tmp, h->stream));
+  OFD_CUDA(cudaStreamSynchronize(h->stream));
+  return OFD_OK;
+}
+
+int ofd_zero_fields(ofd_handle *h) {
+  if (!h) return fail(OFD_EINVAL, "null handle");
+  OFD_CUDA(cudaMemsetAsync(h->fields_raw, 0, h->field_bytes * NF, h->stream));
+  return OFD_OK;
+}
+
+int ofd_set_source(ofd_handle *h, int sx, int sy, int sz, const float *wavelet, int nt) {
+  if (!h) return fail(OFD_EINVAL, "null handle");
+  const Geom &g = h->s.g;
+  if (nt <= 0 || !wavelet) {
+    h->s.src_off = -1;
+    return OFD_OK;
+  }
+  if (sx < 0 || sx >= g.n1 || sy < 0 || sy >= g.n2 || sz < 0 || sz >= g.n3)
+    return fail(OFD_EINVAL, "source (%d,%d,%d) outside the grid", sx, sy, sz);
+  if (h->s.d_wav) {
+    OFD_CUDA(cudaStreamSynchronize(h->stream));
+    cudaFree(h->s.d_wav);
+    h->s.d_wav = nullptr;
+  }
+  OFD_CUDA(cudaMalloc((void **)&h->s.d_wav, sizeof(float) * nt));
+  OFD_CUDA(cudaMemcpy(h->s.d_wav, wavelet, sizeof(float) * nt, cudaMemcpyHostToDevice));
+  h->s.nt = nt;
+  h->s.src_off = (long)sx * g.plane + (long)sy * g.P + sz;
+  return OFD_OK;
+}
+
+int ofd_apply_boundary_init(ofd_handle *h, int level) {
+  if (!h) return fail(OFD_EINVAL, "null handle");
+  if (level < 0 || level > 1) return fail(OFD_EINVAL, "bad level %d", level);
+  h->be->boundary_init(h->s, level, h->stream);
+  OFD_CUDA(cudaGetLastError());
+  return OFD_OK;
+}
+
+int ofd_set_step(ofd_handle *h, long steps) {
+  if (!h || steps < 0) return fail(OFD_EINVAL, "bad argument");
+  h->steps = steps;
+  OFD_CUDA(cudaMemcpyAsync(h->s.d_step, &h->steps, sizeof(long), cudaMemcpyHostToDevice, h->stream));
+  OFD_CUDA(cudaStreamSynchronize(h->stream));
+  return OFD_OK;
+}
+
+int ofd_get_step(ofd_handle *h, long *steps) {
+  if (!h || !steps) return fail(OFD_EINVAL, "bad argument");
+  *steps = h->steps;
+  return OFD_OK;
+}
+
+int ofd_step(ofd_handle *h, int nsteps) {
+  if (!h) return fail(OFD_EINVAL, "null handle");
+  if (nsteps < 0) return fail(OFD_EINVAL, "nsteps < 0");
+  for (int i = 0; i < nsteps; ++i) {
+    const int t0 = (int)(h->steps & 1);
+    h->be->step(h->s, t0, h->stream);
+    h->steps += 1;
+  }
+  OFD_CUDA(cudaGetLastError());
+  return OFD_OK;
+}
+
+int ofd_sync(ofd_handle *h) {
+  if (!h) return fail(OFD_EINVAL, "null handle");
+  OFD_CUDA(cudaStreamSynchronize(h->stream));
+  return OFD_OK;
+}
+
+int ofd_field_sumsq(ofd_handle *h, int level, double out[9]) {
+  if (!h || !out) return fail(OFD_EINVAL, "null argument");
+  if (level < 0 || level > 1) return fail(OFD_EINVAL, "bad level %d", level);
+  h->be->sumsq(h->s, level, h->d_out, h->stream);
+  OFD_CUDA(cudaGetLastError());
+  OFD_CUDA(cudaMemcpyAsync(out, h->d_out, sizeof(double) * NF, cudaMemcpyDeviceToHost, h->stream));
+  OFD_CUDA(cudaStreamSynchronize(h->stream));
+  return OFD_OK;
+}
+
+int ofd_field_view_get(ofd_handle *h, int field, int level, ofd_field_view *out) {
+  int rc = check_fl(h, field, level);
+  if (rc) return rc;
+  if (!out) return fail(OFD_EINVAL, "null out");
+  out->base = (char *)h->s.field[field] + (size_t)level * h->s.g.level * h->s.esize;
+  out->pitch = h->s.g.P;
+  out->storage = h->s.storage;
+  out->scale = h->s.scale[field];
+  return OFD_OK;
+}
+
+}  // extern "C"

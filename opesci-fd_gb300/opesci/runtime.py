@@ -1,0 +1,246 @@
+"""ctypes binding of the device runtime libofd.so (include/ofd.h).
+
+``Simulation`` owns one device handle: nine fields (two time levels) and the
+effective media resident in HBM, advanced with ``step``.  There is no CPU
+path: if the library is missing or no GPU is visible the calls raise."""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+__all__ = ['OFDError', 'load_library', 'Simulation', 'FIELDS', 'STORAGE', 'BC',
+           'config_from_grid', 'library_path']
+
+FIELDS = ['U', 'V', 'W', 'Txx', 'Tyy', 'Tzz', 'Txy', 'Tyz', 'Txz']
+STORAGE = {'f32': 0, 'float': 0, 'fp32': 0, 'f16': 1, 'fp16': 1, 'half': 1,
+           'bf16': 2, 'bfloat16': 2, 'f64': 3, 'double': 3, 'fp64': 3}
+BC = {'none': 0, 'levander': 1, 'robertsson': 2}
+
+
+class OFDError(RuntimeError):
+    """A libofd call returned an error status."""
+
+
+class ofd_config(ctypes.Structure):
+    _fields_ = [('dim', ctypes.c_int * 3),
+                ('space_order', ctypes.c_int),
+                ('storage', ctypes.c_int),
+                ('legacy_bc', ctypes.c_int),
+                ('free_surface', ctypes.c_int * 6),
+                ('spacing', ctypes.c_double * 3),
+                ('dt', ctypes.c_double),
+                ('weights', ctypes.c_double * 4),
+                ('field_scale', ctypes.c_float * 9),
+                ('kernel_variant', ctypes.c_int)]
+
+
+class ofd_field_view(ctypes.Structure):
+    _fields_ = [('base', ctypes.c_void_p), ('pitch', ctypes.c_long),
+                ('storage', ctypes.c_int), ('scale', ctypes.c_float)]
+
+
+_lib = None
+
+
+def library_path():
+    return _build.LIBNAME
+
+
+def load_library():
+    """Load lib/libofd.so.  The library is built by ``__graft_entry__.build()``
+    (or ``python opesci-fd_gb300/opesci/build.py``); a missing library is an
+    error, never a fallback."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIBNAME
+    if not os.path.exists(path):
+        raise OFDError('libofd.so not built (%s); run __graft_entry__.build()' % path)
+    lib = ctypes.CDLL(path, mode=ctypes.RTLD_GLOBAL)
+    P = ctypes.POINTER
+    h = ctypes.c_void_p
+    fptr = P(ctypes.c_float)
+    sig = {
+        'ofd_create': [P(ofd_config), P(h)],
+        'ofd_destroy': [h],
+        'ofd_footprint': [P(ofd_config), P(ctypes.c_size_t)],
+        'ofd_set_media_const': [h, ctypes.c_float, ctypes.c_float, ctypes.c_float],
+        'ofd_set_media': [h, fptr, fptr, fptr],
+        'ofd_upload_field': [h, ctypes.c_int, ctypes.c_int, fptr],
+        'ofd_download_field': [h, ctypes.c_int, ctypes.c_int, fptr],
+        'ofd_upload_field_device': [h, ctypes.c_int, ctypes.c_int, ctypes.c_void_p],
+        'ofd_download_field_device': [h, ctypes.c_int, ctypes.c_int, ctypes.c_void_p],
+        'ofd_zero_fields': [h],
+        'ofd_set_source': [h, ctypes.c_int, ctypes.c_int, ctypes.c_int, fptr, ctypes.c_int],
+        'ofd_apply_boundary_init': [h, ctypes.c_int],
+        'ofd_step': [h, ctypes.c_int],
+        'ofd_sync': [h],
+        'ofd_get_step': [h, P(ctypes.c_long)],
+        'ofd_set_step': [h, ctypes.c_long],
+        'ofd_field_sumsq': [h, ctypes.c_int, P(ctypes.c_double)],
+        'ofd_field_view_get': [h, ctypes.c_int, ctypes.c_int, P(ofd_field_view)],
+    }
+    for name, args in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = ctypes.c_int
+    lib.ofd_last_error.argtypes = []
+    lib.ofd_last_error.restype = ctypes.c_char_p
+    lib.ofd_stream.argtypes = [h]
+    lib.ofd_stream.restype = ctypes.c_void_p
+    _lib = lib
+    return lib
+
+
+def _check(rc, what):
+    if rc != 0:
+        msg = _lib.ofd_last_error().decode(errors='replace')
+        raise OFDError('%s failed (%d): %s' % (what, rc, msg))
+
+
+def _fptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+def make_config(dims, space_order, spacing, dt, weights, storage='f32', free_surface=None,
+                legacy_bc=False, field_scale=None, kernel_variant=0):
+    cfg = ofd_config()
+    for i in range(3):
+        cfg.dim[i] = int(dims[i])
+        cfg.spacing[i] = float(spacing[i])
+    cfg.space_order = int(space_order)
+    cfg.storage = STORAGE[storage] if isinstance(storage, str) else int(storage)
+    cfg.legacy_bc = 1 if legacy_bc else 0
+    fs = free_surface if free_surface is not None else [0] * 6
+    for i in range(6):
+        v = fs[i]
+        cfg.free_surface[i] = BC[v] if isinstance(v, str) else int(v)
+    cfg.dt = float(dt)
+    for k in range(4):
+        cfg.weights[k] = float(weights[k]) if k < len(weights) else 0.0
+    for f in range(9):
+        cfg.field_scale[f] = float(field_scale[f]) if field_scale is not None else 1.0
+    cfg.kernel_variant = int(kernel_variant)
+    return cfg
+
+
+def config_from_grid(grid, storage=None, kernel_variant=0, field_scale=None):
+    """ofd_config of a solved StaggeredGrid: dims, margin, spacing, dt, the
+    staggered weights of its space order, per-face free-surface algorithms."""
+    faces = [0] * 6
+    fs = getattr(grid, 'free_surface', {})
+    for (dim, side), algo in fs.items():
+        faces[2 * (dim - 1) + side] = BC[algo]
+    if storage is None:
+        storage = 'f64' if grid.double else 'f32'
+    return make_config([d.value for d in grid.dim], grid.order[1], [s.value for s in grid.spacing],
+                       grid.dt.value, grid.fd_weights(), storage=storage, free_surface=faces,
+                       legacy_bc=getattr(grid, 'legacy_bc', False), field_scale=field_scale,
+                       kernel_variant=kernel_variant)
+
+
+class Simulation(object):
+    """One device-resident elastic simulation (a libofd handle)."""
+
+    def __init__(self, cfg):
+        self.lib = load_library()
+        self.cfg = cfg
+        self.dims = tuple(cfg.dim[i] for i in range(3))
+        self.h = ctypes.c_void_p()
+        _check(self.lib.ofd_create(ctypes.byref(cfg), ctypes.byref(self.h)), 'ofd_create')
+
+    @staticmethod
+    def footprint(cfg):
+        lib = load_library()
+        n = ctypes.c_size_t()
+        _check(lib.ofd_footprint(ctypes.byref(cfg), ctypes.byref(n)), 'ofd_footprint')
+        return n.value
+
+    def close(self):
+        if self.h:
+            self.lib.ofd_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _arr(self, a):
+        a = np.ascontiguousarray(a, dtype=np.float32)
+        if a.shape != self.dims:
+            a = a.reshape(self.dims)
+        return a
+
+    def set_media_const(self, beta, lam, mu):
+        _check(self.lib.ofd_set_media_const(self.h, beta, lam, mu), 'ofd_set_media_const')
+
+    def set_media(self, rho, vp, vs):
+        r, p, s = self._arr(rho), self._arr(vp), self._arr(vs)
+        _check(self.lib.ofd_set_media(self.h, _fptr(r), _fptr(p), _fptr(s)), 'ofd_set_media')
+
+    def upload(self, field, level, array):
+        f = FIELDS.index(field) if isinstance(field, str) else field
+        a = self._arr(array)
+        _check(self.lib.ofd_upload_field(self.h, f, level, _fptr(a)), 'ofd_upload_field')
+
+    def download(self, field, level=None):
+        f = FIELDS.index(field) if isinstance(field, str) else field
+        if level is None:
+            level = self.steps % 2
+        out = np.empty(self.dims, dtype=np.float32)
+        _check(self.lib.ofd_download_field(self.h, f, level, _fptr(out)), 'ofd_download_field')
+        return out
+
+    def zero(self):
+        _check(self.lib.ofd_zero_fields(self.h), 'ofd_zero_fields')
+
+    def set_source(self, pos, wavelet):
+        w = np.ascontiguousarray(wavelet, dtype=np.float32)
+        _check(self.lib.ofd_set_source(self.h, int(pos[0]), int(pos[1]), int(pos[2]), _fptr(w), len(w)),
+               'ofd_set_source')
+
+    def boundary_init(self, level=0):
+        _check(self.lib.ofd_apply_boundary_init(self.h, level), 'ofd_apply_boundary_init')
+
+    def step(self, n=1):
+        _check(self.lib.ofd_step(self.h, int(n)), 'ofd_step')
+
+    def sync(self):
+        _check(self.lib.ofd_sync(self.h), 'ofd_sync')
+
+    @property
+    def steps(self):
+        v = ctypes.c_long()
+        _check(self.lib.ofd_get_step(self.h, ctypes.byref(v)), 'ofd_get_step')
+        return v.value
+
+    @steps.setter
+    def steps(self, n):
+        _check(self.lib.ofd_set_step(self.h, int(n)), 'ofd_set_step')
+
+    def sumsq(self, level=None):
+        if level is None:
+            level = self.steps % 2
+        out = (ctypes.c_double * 9)()
+        _check(self.lib.ofd_field_sumsq(self.h, level, out), 'ofd_field_sumsq')
+        return np.array(list(out))
+
+    @property
+    def stream(self):
+        return self.lib.ofd_stream(self.h)
+
+    def view(self, field, level):
+        v = ofd_field_view()
+        f = FIELDS.index(field) if isinstance(field, str) else field
+        _check(self.lib.ofd_field_view_get(self.h, f, level, ctypes.byref(v)), 'ofd_field_view_get')
+        return v

@@ -1,0 +1,53 @@
+"""The C ABI library: it loads and exports every entry point include/ofd.h
+declares; host-side validation works without a GPU.  No compute calls."""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    out = set()
+    for name in os.listdir(os.path.join(ROOT, 'include')):
+        if name.endswith('.h'):
+            txt = open(os.path.join(ROOT, 'include', name)).read()
+            out |= set(re.findall(r'\b(ofd_[a-z0-9_]+)\s*\(', txt))
+    return out
+
+
+@pytest.fixture(scope='module')
+def lib():
+    from opesci import build, runtime
+    build.build()
+    return runtime.load_library()
+
+
+def test_library_exports_declared_symbols(lib):
+    syms = declared_symbols()
+    assert len(syms) >= 20
+    path = os.path.join(ROOT, 'opesci-fd_gb300', 'lib', 'libofd.so')
+    nm = subprocess.run(['nm', '-D', '--defined-only', path], capture_output=True, text=True).stdout
+    exported = set(l.split()[-1] for l in nm.splitlines() if ' T ' in l)
+    missing = syms - exported
+    assert not missing, missing
+    for s in syms:
+        assert hasattr(lib, s)
+
+
+def test_footprint_and_validation_without_gpu(lib):
+    from opesci import runtime
+    cfg = runtime.make_config([68, 68, 68], 4, [0.1] * 3, 1e-3, [9 / 8, -1 / 24])
+    n = runtime.Simulation.footprint(cfg)
+    # 9 fields x 2 levels + 8 media, padded rows of 128 floats
+    assert n >= (9 * 2 + 8) * 68 * 68 * 68 * 4
+    bad = runtime.make_config([68, 68, 68], 5, [0.1] * 3, 1e-3, [1.0])
+    with pytest.raises(runtime.OFDError, match='space_order'):
+        runtime.Simulation.footprint(bad)
+    small = runtime.make_config([6, 68, 68], 4, [0.1] * 3, 1e-3, [1.0, 0.0])
+    with pytest.raises(runtime.OFDError, match='too small'):
+        runtime.Simulation.footprint(small)
+    assert 'too small' in lib.ofd_last_error().decode()

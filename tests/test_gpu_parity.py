@@ -1,0 +1,143 @@
+"""GPU parity: the CUDA device runtime (libofd, called through its C ABI)
+against the oracle, the reference-shaped C++ program run on the CPU.
+
+Tolerance: FP32, every field within 1e-5 relative L2 of the oracle after the
+run.  The eigenmode's shear stresses are zero analytically; their computed
+values are rounding residue of cancelling velocity differences, so for those
+three fields the difference is measured relative to the norm of the whole
+stress family (Txx..Txz) instead of their own near-zero norm.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from opesci import runtime
+from opesci.models import eigenwave_grid, initial_fields, l2_error, layered_problem
+from oracle import run as orun
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), 'golden')
+TOL = 1e-5
+SHEAR = ('Txy', 'Tyz', 'Txz')
+STRESS = ('Txx', 'Tyy', 'Tzz', 'Txy', 'Tyz', 'Txz')
+
+
+def run_eigen_gpu(g, variant=0, storage=None, steps=None):
+    sim = runtime.Simulation(runtime.config_from_grid(g, kernel_variant=variant, storage=storage))
+    dv = g.defined_variable
+    sim.set_media_const(dv['beta'].value, dv['lambda'].value, dv['mu'].value)
+    for k, v in initial_fields(g).items():
+        sim.upload(k, 0, v)
+    sim.boundary_init(0)
+    sim.step(steps if steps is not None else g.ntsteps.value)
+    sim.sync()
+    out = {f: sim.download(f) for f in runtime.FIELDS}
+    sim.close()
+    return out
+
+
+def run_problem_gpu(g, media, src, wav, variant=0, storage='f32'):
+    sim = runtime.Simulation(runtime.config_from_grid(g, kernel_variant=variant, storage=storage))
+    sim.set_media(*media)
+    sim.set_source(src, wav)
+    sim.step(g.ntsteps.value)
+    sim.sync()
+    out = {f: sim.download(f) for f in runtime.FIELDS}
+    sim.close()
+    return out
+
+
+def rel_errors(got, ref, shear_by_family=False):
+    fam = np.sqrt(sum(np.linalg.norm(ref[f].astype(np.float64)) ** 2 for f in STRESS))
+    out = {}
+    for f in runtime.FIELDS:
+        a, b = got[f].astype(np.float64), ref[f].astype(np.float64)
+        den = fam if (shear_by_family and f in SHEAR) else np.linalg.norm(b)
+        out[f] = float(np.linalg.norm(a - b) / max(den, 1e-300))
+    return out
+
+
+@pytest.mark.parametrize('so,n,steps', [(4, 32, 100), (8, 32, 60), (2, 24, 60), (6, 24, 60)])
+def test_eigenwave_matches_oracle(tmp_path, so, n, steps):
+    g = eigenwave_grid(grid_size=(n, n, n), ntsteps=steps, space_order=so)
+    got = run_eigen_gpu(g)
+    ref = orun.run(g, str(tmp_path))
+    errs = rel_errors(got, ref['fields'], shear_by_family=True)
+    assert max(errs.values()) < TOL, errs
+    # analytic-solution error norms, FP64 on both sides
+    for f in g.fields:
+        name = f.label.name
+        e_gpu = l2_error(g, f, got[name])
+        assert abs(e_gpu - ref['l2_fp64'][name]) <= 1e-4 * ref['l2_fp64'][name] + 1e-12, name
+
+
+@pytest.mark.parametrize('so', [4, 8])
+def test_heterogeneous_source_matches_oracle(tmp_path, so):
+    files = {k: str(tmp_path / (k + '.raw')) for k in ('rho', 'vp', 'vs')}
+    g, media, src, wav = layered_problem(40, space_order=so, ntsteps=120, seed=11, media_files=files)
+    got = run_problem_gpu(g, media, src, wav)
+    ref = orun.run(g, str(tmp_path), source=(src, wav))
+    errs = rel_errors(got, ref['fields'])
+    assert max(errs.values()) < TOL, errs
+    assert np.abs(got['Txx']).max() > 0
+
+
+def test_legacy_gpu_reproduces_reference_test3d(tmp_path):
+    """The reference's own program benchmarks/test3d.cpp (100^3, 1000 steps):
+    GPU fields against the legacy oracle, and GPU error norms against the
+    norms the reference binary printed.  The reference accumulates its norms
+    in float (staggeredgrid.py:916), which by itself moves them by ~1e-3
+    relative from the exact sum, so that last comparison uses 2e-3."""
+    gold = json.load(open(os.path.join(GOLDEN, 'test3d_l2.json')))
+    g = eigenwave_grid(grid_size=(100, 100, 100), dt=0.002, ntsteps=1000, legacy=True)
+    got = run_eigen_gpu(g)
+    ref = orun.run(g, str(tmp_path), legacy=True)
+    errs = rel_errors(got, ref['fields'], shear_by_family=True)
+    assert max(errs.values()) < TOL, errs
+    for f in g.fields:
+        name = f.label.name
+        e = l2_error(g, f, got[name])
+        assert abs(e - ref['l2_fp64'][name]) < 1e-4 * ref['l2_fp64'][name], name
+        assert abs(e - gold['l2'][name]) < 2e-3 * gold['l2'][name], (name, e, gold['l2'][name])
+
+
+def test_plain_and_best_kernels_agree():
+    g, media, src, wav = layered_problem(72, space_order=4, ntsteps=40, seed=5)
+    a = run_problem_gpu(g, media, src, wav, variant=0)
+    b = run_problem_gpu(g, media, src, wav, variant=1)
+    errs = rel_errors(a, b)
+    assert max(errs.values()) < 1e-6, errs
+
+
+def test_steps_are_resumable():
+    """Advancing 30 steps in three calls equals one call of 30 (the
+    time-slice mechanism serving relies on)."""
+    g, media, src, wav = layered_problem(32, space_order=4, ntsteps=30, seed=2)
+    a = run_problem_gpu(g, media, src, wav)
+    sim = runtime.Simulation(runtime.config_from_grid(g))
+    sim.set_media(*media)
+    sim.set_source(src, wav)
+    for n in (7, 13, 10):
+        sim.step(n)
+    sim.sync()
+    b = {f: sim.download(f) for f in runtime.FIELDS}
+    sim.close()
+    for f in runtime.FIELDS:
+        assert np.array_equal(a[f], b[f]), f
+
+
+def test_error_paths_leave_context_usable():
+    from opesci.runtime import OFDError
+    g, media, src, wav = layered_problem(24, space_order=4, ntsteps=5, seed=1)
+    sim = runtime.Simulation(runtime.config_from_grid(g))
+    with pytest.raises(OFDError, match='outside'):
+        sim.set_source((10000, 1, 1), wav)
+    with pytest.raises(OFDError, match='bad field'):
+        sim.download(42, 0)
+    sim.set_media(*media)
+    sim.step(5)
+    sim.sync()
+    assert np.isfinite(sim.sumsq()).all()
+    sim.close()
