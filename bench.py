@@ -1,0 +1,301 @@
+"""Benchmark of the elastic velocity-stress hot path on GB300.
+
+Workload: one time step (stress sweep, stress ghosts, velocity sweep,
+velocity ghosts, source) of the 9-field elastic staggered-grid scheme on a
+512^3 interior grid, space order 4, FP32, seeded layered heterogeneous medium
+(20 layers, vp U[1.5,4.5] km/s, 5% smoothed perturbation, vs = vp/sqrt(3),
+Gardner density), 10 m spacing, 15 Hz Ricker source, dt = 0.5 x stable step.
+All inputs are synthetic and seeded.  The 18 field levels + 8 media arrays
+(~15 GB) are far larger than L2, so no explicit flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line.  Under torchrun each rank runs an independent replica
+(the path has no exchange step); value is the sum over ranks of grid-point
+updates divided by the slowest rank's time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, 'opesci-fd_gb300')):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = 'elastic GLUP/s (grid-point updates of all 9 fields per second), 512^3 SO4 FP32 heterogeneous'
+UNIT = 'GLUP/s'
+# algorithmic bytes per grid point of each sweep (FP32 fields, FP32 media):
+# stress reads U V W + 6 stresses + lambda mu mu12 mu13 mu23, writes 6 stresses
+# velocity reads U V W + 6 stresses + beta1..3, writes U V W
+STRESS_BYTES_PER_LUP = 4 * (9 + 5 + 6)
+VELOCITY_BYTES_PER_LUP = 4 * (9 + 3 + 3)
+STEP_BYTES_PER_LUP = STRESS_BYTES_PER_LUP + VELOCITY_BYTES_PER_LUP
+
+
+def dist_env():
+    rank = int(os.environ.get('RANK', '0'))
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    return rank, world, local
+
+
+def measured_peak():
+    p = os.path.join(ROOT, 'MEASURED_PEAKS.json')
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d['hbm_gbs']), 'measured (MEASURED_PEAKS.json hbm_gbs)'
+    return 6800.0, 'fallback 6.8 TB/s'
+
+
+def profiled_traffic(kind):
+    """DRAM bytes per grid point of a kernel from the committed ncu summary
+    (profiles/traffic.txt lines '<kernel> <bytes_per_lup>'), or None."""
+    p = os.path.join(ROOT, 'profiles', 'traffic.txt')
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        parts = line.split()
+        if len(parts) >= 2 and parts[0] == kind:
+            try:
+                return float(parts[1])
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler(object):
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed
+    region (200 ms period)."""
+
+    FIELDS = ('clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+              'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+              'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix='.csv')
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ['nvidia-smi', '-i', str(self.index), '--query-gpu=' + self.FIELDS,
+                 '--format=csv,noheader,nounits', '-lms', '200'],
+                stdout=open(self.path, 'w'), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(',')]
+            if len(p) >= 8:
+                rows.append(p)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[0]) for r in rows if r[0].replace('.', '').isdigit()]
+        mx = [float(r[1]) for r in rows if r[1].replace('.', '').isdigit()]
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[4 + i].lower() == 'active'})
+        return {'sm_mhz': statistics.median(sm) if sm else None,
+                'sm_max_mhz': max(mx) if mx else None,
+                'reasons': reasons, 'samples': len(rows)}
+
+
+def build_problem(n, so, steps, seed=0):
+    from opesci.models import layered_problem
+    return layered_problem(n, space_order=so, ntsteps=steps, seed=seed)
+
+
+def cpu_oracle(n, so, steps, seed=0, threads=None):
+    """Time the reference-shaped generated C++ (the oracle program: the
+    reference's generator output for this model, reference GNU flags) on the
+    host cores for ``steps`` steps of an n^3 problem of the same kind."""
+    from opesci.models import layered_problem
+    from oracle import run as orun
+    with tempfile.TemporaryDirectory() as d:
+        files = {k: os.path.join(d, k + '.raw') for k in ('rho', 'vp', 'vs')}
+        g, media, src, wav = layered_problem(n, space_order=so, ntsteps=steps, seed=seed, media_files=files)
+        out = orun.run(g, d, source=(src, wav), threads=threads, dump=False)
+    lups = float(n) ** 3 * steps
+    return lups / out['loop_seconds'] / 1e9, out['threads'], out['loop_seconds']
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    n = args.size if args.ref_size is None else args.ref_size
+    steps = max(1, min(args.steps, args.ref_steps))
+    val, cores, secs = cpu_oracle(n, args.space_order, steps)
+    line = {
+        'impl': 'reference', 'metric': METRIC, 'value': val, 'unit': UNIT,
+        'n_gpus': 0, 'steps': steps, 'warmup': 0, 'ms_per_step': secs * 1e3 / steps,
+        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
+        'data': 'synthetic (seeded layered medium, Ricker source)',
+        'config': {'workload': 'elastic %d^3 SO%d FP32 heterogeneous + Ricker source, free surfaces' % (n, args.space_order),
+                   'grid': [n, n, n], 'space_order': args.space_order, 'l2_flush': 'inputs larger than L2'},
+        'cpu_baseline': {'value': val, 'unit': UNIT, 'cores': cores, 'kind': 'port',
+                         'sample': '%d steps of the %d^3 problem, reference-shaped generated C++ '
+                                   '(g++ -g -O3 -fno-tree-vectorize -fopenmp), time loop only' % (steps, n)},
+        'e2e': {'value': val, 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=200)
+    ap.add_argument('--warmup', type=int, default=5)
+    ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
+    ap.add_argument('--size', type=int, default=512)
+    ap.add_argument('--space-order', type=int, default=4)
+    ap.add_argument('--storage', default='f32')
+    ap.add_argument('--variant', type=int, default=0)
+    ap.add_argument('--ref-size', type=int, default=None)
+    ap.add_argument('--ref-steps', type=int, default=10)
+    ap.add_argument('--cpu-size', type=int, default=256)
+    ap.add_argument('--cpu-steps', type=int, default=20)
+    ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--no-e2e', action='store_true')
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank, world, local = dist_env()
+
+    if args.impl == 'reference':
+        run_reference(args, rank)
+        return
+
+    import ctypes
+    import numpy as np
+    from opesci import runtime
+
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group('nccl')
+    else:
+        runtime.load_library()
+
+    n, so = args.size, args.space_order
+    g, media, src, wav = build_problem(n, so, args.warmup + args.steps)
+    cfg = runtime.config_from_grid(g, storage=args.storage, kernel_variant=args.variant)
+    sim = runtime.Simulation(cfg)
+    sim.set_coefficients_from_grid(g)
+    sim.set_media(*media)
+    sim.set_source(src, wav)
+    sim.step(args.warmup)
+    sim.sync()
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    if dist is not None:
+        dist.barrier()
+    sim.sync()
+    total_ms, cls_ms, launches = sim.step_profiled(args.steps)
+    sim.sync()
+    if dist is not None:
+        dist.barrier()
+    clocks = sampler.stop()
+    ms = total_ms
+    if dist is not None:
+        import torch
+        t = torch.tensor([ms], dtype=torch.float64, device='cuda')
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    lups_rank = float(n) ** 3 * args.steps
+    value = lups_rank * world / (ms / 1e3) / 1e9
+
+    peak, peak_src = measured_peak()
+    stress_ms = cls_ms[0] / args.steps
+    vel_ms = cls_ms[2] / args.steps
+    esz = {'f32': 4, 'f16': 2, 'bf16': 2, 'f64': 8}.get(args.storage, 4)
+    sb = (9 + 6) * esz + 5 * 4
+    vb = (9 + 3) * esz + 3 * 4
+    stress_bytes = float(n) ** 3 * sb
+    achieved = stress_bytes / (stress_ms / 1e3) / 1e9
+    tr = profiled_traffic('stress_sweep_so%d_%s' % (so, args.storage))
+    roofline = {'bound': 'hbm', 'kernel': 'stress sweep', 'achieved': achieved, 'peak': peak,
+                'unit': 'GB/s', 'frac': achieved / peak, 'peak_source': peak_src,
+                'traffic': (tr * float(n) ** 3) if tr else None,
+                'algorithmic_bytes_per_launch': stress_bytes,
+                'avg_launch_ms': stress_ms,
+                'velocity_sweep': {'achieved': float(n) ** 3 * vb / (vel_ms / 1e3) / 1e9, 'avg_launch_ms': vel_ms},
+                'step': {'bytes_per_lup': sb + vb,
+                         'achieved': float(n) ** 3 * (sb + vb) * args.steps / (ms / 1e3) / 1e9},
+                'class_ms_per_step': [c / args.steps for c in cls_ms]}
+
+    e2e = None
+    if not args.no_e2e:
+        # the C-ABI job as a user runs it: host media in, K steps, 9 host fields out
+        host_fields = [np.empty(sim.dims, dtype=np.float32) for _ in range(9)]
+        sim.sync()
+        t0 = time.perf_counter()
+        sim.zero()
+        sim.steps = 0
+        sim.set_media(*media)
+        sim.set_source(src, wav)
+        sim.step(args.steps)
+        lvl = args.steps % 2
+        for i in range(9):
+            sim.lib.ofd_download_field(sim.h, i, lvl, host_fields[i].ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+        sim.sync()
+        wall = time.perf_counter() - t0
+        cells = float(np.prod(sim.dims))
+        e2e = {'value': lups_rank / wall / 1e9, 'unit': UNIT,
+               'h2d_bytes_per_step': (3 * cells * 4 + len(wav) * 4) / args.steps,
+               'd2h_bytes_per_step': 9 * cells * 4 / args.steps,
+               'note': 'one job through the C ABI from host buffers: media upload + effective media, '
+                       'K steps, download of the 9 final fields'}
+    sim.close()
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        try:
+            v, cores, secs = cpu_oracle(args.cpu_size, so, args.cpu_steps)
+            cpu = {'value': v, 'unit': UNIT, 'cores': cores, 'kind': 'port',
+                   'sample': '%d steps of a %d^3 problem of the same kind (SO%d, heterogeneous, source), '
+                             'reference-shaped generated C++ (g++ -g -O3 -fno-tree-vectorize -fopenmp), '
+                             'time loop only, %.1f s' % (args.cpu_steps, args.cpu_size, so, secs)}
+        except Exception as e:  # report, do not hide
+            cpu = {'value': None, 'error': str(e)[:300]}
+
+    if rank == 0:
+        line = {
+            'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
+            'warmup': args.warmup, 'ms_per_step': ms / args.steps, 'higher_is_better': True,
+            'scaling': 'weak', 'vs_baseline': None, 'dtype': args.storage,
+            'data': 'synthetic (seeded layered medium, Ricker source)',
+            'config': {'workload': 'elastic %d^3 SO%d %s heterogeneous + Ricker source, free surfaces' % (n, so, args.storage.upper()),
+                       'grid': [n, n, n], 'space_order': so, 'parallelism': 'replicas x%d' % world,
+                       'l2_flush': 'inputs larger than L2 (%.1f GB resident)' % (runtime.Simulation.footprint(cfg) / 1e9),
+                       'kernel_variant': args.variant},
+            'roofline': roofline, 'cpu_baseline': cpu, 'e2e': e2e, 'clocks': clocks,
+            'gpu_launches': launches,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == '__main__':
+    main()

@@ -77,6 +77,17 @@ int ofd_footprint(const ofd_config *cfg, size_t *bytes);
 int ofd_set_media_const(ofd_handle *h, float beta, float lambda, float mu);
 int ofd_set_media(ofd_handle *h, const float *rho, const float *vp, const float *vs);
 
+/* Literal tables of the generated update expressions (required before
+ * ofd_step).  The sweeps evaluate the reference generator's expanded,
+ * constant-folded stencil expression (staggeredgrid.py:728-748 through
+ * regulargrid.py:329-342 and codeprinter.py) term by term in its printed
+ * order; ks/kv hold the values of its floating literals in order of
+ * appearance, as opesci.templates.cuda_gen.sweep_tables computes them.
+ * het = 1 for media read from arrays (media are factors of each term), 0 for
+ * constant media folded into the literals.  nks/nkv must equal the table
+ * sizes of the prebuilt expression for this space order and media mode. */
+int ofd_set_coefficients(ofd_handle *h, int het, const float *ks, int nks, const float *kv, int nkv);
+
 /* Field transfer, reference layout, host memory (pageable or pinned). */
 int ofd_upload_field(ofd_handle *h, int field, int level, const float *host);
 int ofd_download_field(ofd_handle *h, int field, int level, float *host);
@@ -100,6 +111,12 @@ int ofd_apply_boundary_init(ofd_handle *h, int level);
  * on the handle's stream. */
 int ofd_step(ofd_handle *h, int nsteps);
 int ofd_sync(ofd_handle *h);
+/* ofd_step with CUDA events recorded on the handle's stream around every
+ * kernel class of every step; waits for completion.  ms_total is the time
+ * from the first to the last event; ms_class[k] the summed device time of
+ * class k: 0 stress sweep, 1 stress ghosts, 2 velocity sweep, 3 velocity
+ * ghosts and source.  launches (may be NULL) receives the kernel count. */
+int ofd_step_profiled(ofd_handle *h, int nsteps, double *ms_total, double ms_class[4], long *launches);
 /* completed steps; the newest level is steps % 2 */
 int ofd_get_step(ofd_handle *h, long *steps);
 int ofd_set_step(ofd_handle *h, long steps);

@@ -15,6 +15,8 @@
 #include <cuda_bf16.h>
 #include <stdint.h>
 
+#define OFD_MAX_K 160
+
 namespace ofd {
 
 enum { F_U = 0, F_V, F_W, F_TXX, F_TYY, F_TZZ, F_TXY, F_TYZ, F_TXZ, NF };
@@ -65,6 +67,7 @@ template <typename S> struct SweepArgs {
   typename Storage<S>::C dt, ih1, ih2, ih3;
   typename Storage<S>::C c[4];
   int xchunk;          // planes per CTA along x
+  float K[OFD_MAX_K];  // literal table of the generated update expression
 };
 
 // Ghost-cell launch arguments: one level, per-face algorithm.

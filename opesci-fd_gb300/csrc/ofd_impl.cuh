@@ -28,15 +28,29 @@ struct DevState {
   int variant;         // 0 best, 1 plain
   double *d_partial;   // reduction scratch (>= 2048 doubles)
   long *d_step;        // device step counter (graph-safe source index)
+  TiledCtx tiled;      // TMA descriptors for the tiled sweeps
+  int het;             // 1: media arrays are factors of the update (read mode)
+  int nks, nkv;        // literal-table sizes (0 until ofd_set_coefficients)
+  float Ks[OFD_MAX_K], Kv[OFD_MAX_K];
+};
+
+// Optional per-kernel-class events of a profiled step: ev[2k], ev[2k+1]
+// bracket class k (0 stress sweep, 1 stress ghosts, 2 velocity sweep,
+// 3 velocity ghosts + source).
+struct StepEvents {
+  cudaEvent_t ev[8];
 };
 
 struct Backend {
   virtual ~Backend() {}
-  virtual void step(const DevState &s, int t0, cudaStream_t st) = 0;
+  virtual void step(const DevState &s, int t0, cudaStream_t st, const StepEvents *ev = nullptr) = 0;
+  virtual int launches_per_step(const DevState &s) const = 0;
   virtual void boundary_init(const DevState &s, int level, cudaStream_t st) = 0;
   virtual void to_padded(const DevState &s, const float *dense, int f, int level, cudaStream_t st) = 0;
   virtual void from_padded(const DevState &s, float *dense, int f, int level, cudaStream_t st) = 0;
   virtual void sumsq(const DevState &s, int level, double *d_out9, cudaStream_t st) = 0;
+  // literal-table sizes of the generated expressions for media mode het
+  virtual int table_size(int het, int stress) const = 0;
 };
 
 Backend *make_backend_f32(int R);
@@ -136,6 +150,9 @@ struct Impl : Backend {
     a.ih3 = (C)(1.0 / s.h[2]);
     for (int k = 0; k < 4; ++k) a.c[k] = (C)s.c[k];
     a.xchunk = 0;
+    const float *K = stress ? s.Ks : s.Kv;
+    const int nk = stress ? s.nks : s.nkv;
+    for (int k = 0; k < OFD_MAX_K; ++k) a.K[k] = k < nk ? K[k] : 0.f;
     return a;
   }
 
@@ -191,9 +208,14 @@ struct Impl : Backend {
     SweepArgs<S> a = sweep_args(s, t0, stress);
     const Geom &g = s.g;
     const int nx = g.n1 - 2 * g.m, ny = g.n2 - 2 * g.m, nz = g.n3 - 2 * g.m;
-    if (s.variant != 1 && tiled_supported<R, S>(g)) {
-      if (stress) launch_stress_tiled<R, S>(a, st);
-      else launch_velocity_tiled<R, S>(a, st);
+    if (s.variant != 1 && s.tiled.maps && tiled_supported<R, S>(g)) {
+      if (s.het) {
+        if (stress) launch_stress_tiled<R, S, 1>(a, s.tiled, t0, st);
+        else launch_velocity_tiled<R, S, 1>(a, s.tiled, t0, st);
+      } else {
+        if (stress) launch_stress_tiled<R, S, 0>(a, s.tiled, t0, st);
+        else launch_velocity_tiled<R, S, 0>(a, s.tiled, t0, st);
+      }
       return;
     }
     // plain: aim for >= 4 waves of 152 SMs
@@ -205,15 +227,28 @@ struct Impl : Backend {
     if (chunks > nx) chunks = nx;
     a.xchunk = (nx + chunks - 1) / chunks;
     grd.z = (nx + a.xchunk - 1) / a.xchunk;
-    if (stress) stress_plain<R, S><<<grd, blk, 0, st>>>(a);
-    else velocity_plain<R, S><<<grd, blk, 0, st>>>(a);
+    if (s.het) {
+      if (stress) stress_plain<R, S, 1><<<grd, blk, 0, st>>>(a);
+      else velocity_plain<R, S, 1><<<grd, blk, 0, st>>>(a);
+    } else {
+      if (stress) stress_plain<R, S, 0><<<grd, blk, 0, st>>>(a);
+      else velocity_plain<R, S, 0><<<grd, blk, 0, st>>>(a);
+    }
   }
 
-  void step(const DevState &s, int t0, cudaStream_t st) override {
+  void step(const DevState &s, int t0, cudaStream_t st, const StepEvents *ev) override {
     const int t1 = 1 - t0;
+    auto rec = [&](int i) { if (ev) cudaEventRecord(ev->ev[i], st); };
+    rec(0);
     sweeps(s, t0, true, st);
+    rec(1);
+    rec(2);
     stress_bc(s, t1, t0, s.legacy ? 0 : 1, st);
+    rec(3);
+    rec(4);
     sweeps(s, t0, false, st);
+    rec(5);
+    rec(6);
     velocity_bc(s, t1, st);
     if (s.src_off >= 0) {
       source_kernel<S><<<1, 1, 0, st>>>(fp(s, F_TXX, t1), fp(s, F_TYY, t1), fp(s, F_TZZ, t1), s.src_off,
@@ -221,6 +256,12 @@ struct Impl : Backend {
                                         s.scale[F_TZZ]);
     }
     step_tick<<<1, 1, 0, st>>>(s.d_step);
+    rec(7);
+  }
+
+  int launches_per_step(const DevState &s) const override {
+    // 2 sweeps + 3 stress-ghost phases + 6 velocity-ghost phases + source + tick
+    return 2 + 3 + 6 + (s.src_off >= 0 ? 1 : 0) + 1;
   }
 
   void boundary_init(const DevState &s, int level, cudaStream_t st) override {
@@ -234,6 +275,11 @@ struct Impl : Backend {
 
   void from_padded(const DevState &s, float *dense, int f, int level, cudaStream_t st) override {
     padded_to_dense<S><<<1216, 256, 0, st>>>(fp(s, f, level), dense, s.g, 1.f / s.scale[f]);
+  }
+
+  int table_size(int het, int stress) const override {
+    if (het) return stress ? GenSweep<R, 1>::NK_STRESS : GenSweep<R, 1>::NK_VELOCITY;
+    return stress ? GenSweep<R, 0>::NK_STRESS : GenSweep<R, 0>::NK_VELOCITY;
   }
 
   void sumsq(const DevState &s, int level, double *d_out9, cudaStream_t st) override {

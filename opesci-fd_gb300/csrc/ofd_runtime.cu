@@ -7,6 +7,8 @@
 #include <string>
 #include <vector>
 
+#include <cuda.h>
+
 #include "ofd.h"
 #include "ofd_impl.cuh"
 
@@ -94,6 +96,8 @@ struct ofd_handle {
   long level_elems = 0;         // elements of one field level (padded)
   long steps = 0;
   double *d_out = nullptr;      // 16 doubles
+  int *d_err = nullptr;         // error word of bounded device waits
+  TmaMaps *maps = nullptr;      // TMA descriptors (host copy)
 };
 
 namespace {
@@ -162,6 +166,53 @@ Geom media_geom(const ofd_config *c, int *z0) {
   Layout L = make_layout(&f);
   *z0 = L.z0;
   return L.g;
+}
+
+CUtensorMapDataType tma_type(int storage) {
+  switch (storage) {
+    case OFD_F16: return CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
+    case OFD_BF16: return CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+    case OFD_F64: return CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+  }
+  return CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+}
+
+// 3D descriptor over one level: dims (P, n2, n1), rows of P elements.
+bool encode(CUtensorMap *m, void *level_base, CUtensorMapDataType t, size_t es, const Geom &g, int bw, int bh) {
+  cuuint64_t dims[3] = {(cuuint64_t)g.P, (cuuint64_t)g.n2, (cuuint64_t)g.n1};
+  cuuint64_t strides[2] = {(cuuint64_t)(g.P * es), (cuuint64_t)(g.plane * es)};
+  cuuint32_t box[3] = {(cuuint32_t)bw, (cuuint32_t)bh, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = cuTensorMapEncodeTiled(m, t, 3, level_base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                      CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+// Descriptors for every field level (halo and point boxes) and media array.
+// Returns false (tiled path off) if any encoding is rejected.
+bool build_maps(ofd_handle *h) {
+  TmaMaps *mp = new TmaMaps();
+  const Geom &g = h->s.g;
+  int hw, hh, pw, ph;
+  tiled_boxes(h->s.R, (int)h->s.esize, &hw, &hh, &pw, &ph);
+  const CUtensorMapDataType t = tma_type(h->s.storage);
+  bool ok = hw <= 256 && hh <= 256;
+  for (int f = 0; f < NF && ok; ++f)
+    for (int l = 0; l < 2 && ok; ++l) {
+      char *base = (char *)h->s.field[f] - (size_t)h->s.z0 * h->s.esize + (size_t)l * g.level * h->s.esize;
+      ok = encode(&mp->halo[f][l], base, t, h->s.esize, g, hw, hh) &&
+           encode(&mp->point[f][l], base, t, h->s.esize, g, pw, ph);
+    }
+  for (int i = 0; i < NM && ok; ++i)
+    ok = encode(&mp->media[i], (void *)(h->s.media[i] - h->s.z0), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, g, pw, ph);
+  if (!ok) {
+    delete mp;
+    return false;
+  }
+  mp->ok = 1;
+  h->maps = mp;
+  return true;
 }
 
 }  // namespace
@@ -233,6 +284,7 @@ int ofd_create(const ofd_config *cfg, ofd_handle **out) {
   h->s.d_partial = (double *)extra;                    // 2048 doubles = 16 KB? keep 1152 used
   h->s.d_step = (long *)(extra + 2 * 4096 + 1024);
   h->d_out = (double *)(extra + 2 * 4096 + 2048);
+  h->d_err = (int *)(extra + 3 * 4096);
   h->s.d_wav = nullptr;
   h->s.src_off = -1;
   h->s.nt = 0;
@@ -245,12 +297,18 @@ int ofd_create(const ofd_config *cfg, ofd_handle **out) {
   for (int i = 0; i < 3; ++i) h->s.h[i] = cfg->spacing[i];
   for (int k = 0; k < 4; ++k) h->s.c[k] = cfg->weights[k];
   h->s.variant = cfg->kernel_variant;
+  h->s.het = 0;
+  h->s.nks = h->s.nkv = 0;
   switch (cfg->storage) {
     case OFD_F32: h->be = make_backend_f32(h->s.R); break;
     case OFD_F64: h->be = make_backend_f64(h->s.R); break;
     case OFD_F16: h->be = make_backend_f16(h->s.R); break;
     case OFD_BF16: h->be = make_backend_bf16(h->s.R); break;
   }
+  h->s.tiled.maps = nullptr;
+  h->s.tiled.err = h->d_err;
+  h->s.tiled.z0 = L.z0;
+  if (build_maps(h)) h->s.tiled.maps = h->maps;
   e = cudaStreamSynchronize(h->stream);
   if (e != cudaSuccess || !h->be) {
     int code = fail(OFD_ECUDA, "initialisation failed: %s", cudaGetErrorString(e));
@@ -265,6 +323,7 @@ int ofd_destroy(ofd_handle *h) {
   if (!h) return OFD_OK;
   if (h->stream) cudaStreamSynchronize(h->stream);
   delete h->be;
+  delete h->maps;
   if (h->s.d_wav) cudaFree(h->s.d_wav);
   if (h->fields_raw) cudaFree(h->fields_raw);
   if (h->media_raw) cudaFree(h->media_raw);
@@ -274,6 +333,21 @@ int ofd_destroy(ofd_handle *h) {
 }
 
 void *ofd_stream(ofd_handle *h) { return h ? (void *)h->stream : nullptr; }
+
+int ofd_set_coefficients(ofd_handle *h, int het, const float *ks, int nks, const float *kv, int nkv) {
+  if (!h || !ks || !kv) return fail(OFD_EINVAL, "null argument");
+  if (het != 0 && het != 1) return fail(OFD_EINVAL, "het must be 0 or 1");
+  const int es = h->be->table_size(het, 1), ev = h->be->table_size(het, 0);
+  if (nks != es || nkv != ev)
+    return fail(OFD_EINVAL, "coefficient tables of size %d/%d do not match the prebuilt %s expression of space order %d (%d/%d)",
+                nks, nkv, het ? "heterogeneous" : "constant-media", h->cfg.space_order, es, ev);
+  h->s.het = het;
+  h->s.nks = nks;
+  h->s.nkv = nkv;
+  for (int i = 0; i < nks; ++i) h->s.Ks[i] = ks[i];
+  for (int i = 0; i < nkv; ++i) h->s.Kv[i] = kv[i];
+  return OFD_OK;
+}
 
 int ofd_set_media_const(ofd_handle *h, float beta, float lambda, float mu) {
   if (!h) return fail(OFD_EINVAL, "null handle");
@@ -411,6 +485,7 @@ int ofd_get_step(ofd_handle *h, long *steps) {
 int ofd_step(ofd_handle *h, int nsteps) {
   if (!h) return fail(OFD_EINVAL, "null handle");
   if (nsteps < 0) return fail(OFD_EINVAL, "nsteps < 0");
+  if (h->s.nks == 0) return fail(OFD_ESTATE, "ofd_set_coefficients has not been called");
   for (int i = 0; i < nsteps; ++i) {
     const int t0 = (int)(h->steps & 1);
     h->be->step(h->s, t0, h->stream);
@@ -420,10 +495,52 @@ int ofd_step(ofd_handle *h, int nsteps) {
   return OFD_OK;
 }
 
+static int check_err_word(ofd_handle *h) {
+  int err = 0;
+  OFD_CUDA(cudaMemcpyAsync(&err, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  OFD_CUDA(cudaStreamSynchronize(h->stream));
+  if (err) {
+    int zero = 0;
+    cudaMemcpy(h->d_err, &zero, sizeof(int), cudaMemcpyHostToDevice);
+    return fail(OFD_ETIMEOUT, "a bounded device wait expired in a tiled sweep (error word %d)", err);
+  }
+  return OFD_OK;
+}
+
+int ofd_step_profiled(ofd_handle *h, int nsteps, double *ms_total, double ms_class[4], long *launches) {
+  if (!h || !ms_total || !ms_class) return fail(OFD_EINVAL, "null argument");
+  if (nsteps <= 0) return fail(OFD_EINVAL, "nsteps must be > 0");
+  if (h->s.nks == 0) return fail(OFD_ESTATE, "ofd_set_coefficients has not been called");
+  std::vector<StepEvents> evs(nsteps);
+  for (int i = 0; i < nsteps; ++i)
+    for (int k = 0; k < 8; ++k) OFD_CUDA(cudaEventCreate(&evs[i].ev[k]));
+  for (int i = 0; i < nsteps; ++i) {
+    const int t0 = (int)(h->steps & 1);
+    h->be->step(h->s, t0, h->stream, &evs[i]);
+    h->steps += 1;
+  }
+  OFD_CUDA(cudaGetLastError());
+  OFD_CUDA(cudaStreamSynchronize(h->stream));
+  for (int k = 0; k < 4; ++k) ms_class[k] = 0;
+  for (int i = 0; i < nsteps; ++i)
+    for (int k = 0; k < 4; ++k) {
+      float ms = 0;
+      OFD_CUDA(cudaEventElapsedTime(&ms, evs[i].ev[2 * k], evs[i].ev[2 * k + 1]));
+      ms_class[k] += ms;
+    }
+  float tot = 0;
+  OFD_CUDA(cudaEventElapsedTime(&tot, evs[0].ev[0], evs[nsteps - 1].ev[7]));
+  *ms_total = tot;
+  if (launches) *launches = (long)nsteps * h->be->launches_per_step(h->s);
+  for (int i = 0; i < nsteps; ++i)
+    for (int k = 0; k < 8; ++k) cudaEventDestroy(evs[i].ev[k]);
+  return check_err_word(h);
+}
+
 int ofd_sync(ofd_handle *h) {
   if (!h) return fail(OFD_EINVAL, "null handle");
   OFD_CUDA(cudaStreamSynchronize(h->stream));
-  return OFD_OK;
+  return check_err_word(h);
 }
 
 int ofd_field_sumsq(ofd_handle *h, int level, double out[9]) {

@@ -15,8 +15,11 @@ INCLUDE = os.path.join(REPO_ROOT, 'include')
 LIBNAME = os.path.join(LIBDIR, 'libofd.so')
 
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
+# -fmad=false: no multiply-add contraction, so the generated update
+# expressions round exactly like the reference's C code (which g++ does not
+# contract in ISO C++ mode)
 NVCC_FLAGS = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '--expt-relaxed-constexpr',
-              '-Xptxas', '-warn-spills']
+              '-fmad=false', '-Xptxas', '-warn-spills']
 
 
 def nvcc():
@@ -33,7 +36,9 @@ def sources():
 
 
 def _newest_input():
-    paths = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(INCLUDE, 'ofd.h')]
+    paths = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if not os.path.isdir(os.path.join(CSRC, f))]
+    paths += [os.path.join(CSRC, 'generated', f) for f in os.listdir(os.path.join(CSRC, 'generated'))]
+    paths += [os.path.join(INCLUDE, 'ofd.h')]
     return max(os.path.getmtime(p) for p in paths)
 
 

@@ -139,19 +139,9 @@ def ricker(nt, dt, f0):
 
 def _smooth_axis(a, radius, axis):
     # three passes of a box filter of width 2r+1 approximate a Gaussian
+    from scipy.ndimage import uniform_filter1d
     for _ in range(3):
-        c = np.cumsum(a, axis=axis, dtype=np.float64)
-        n = a.shape[axis]
-        pad_shape = list(a.shape)
-        pad_shape[axis] = 1
-        c = np.concatenate([np.zeros(pad_shape), c], axis=axis)
-        lo = np.clip(np.arange(n) - radius, 0, n)
-        hi = np.clip(np.arange(n) + radius + 1, 0, n)
-        s = np.take(c, hi, axis=axis) - np.take(c, lo, axis=axis)
-        w = (hi - lo).astype(np.float64)
-        shape = [1] * a.ndim
-        shape[axis] = n
-        a = (s / w.reshape(shape)).astype(np.float32)
+        a = uniform_filter1d(a, size=2 * radius + 1, axis=axis, mode='nearest')
     return a
 
 

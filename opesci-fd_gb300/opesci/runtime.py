@@ -67,6 +67,7 @@ def load_library():
         'ofd_destroy': [h],
         'ofd_footprint': [P(ofd_config), P(ctypes.c_size_t)],
         'ofd_set_media_const': [h, ctypes.c_float, ctypes.c_float, ctypes.c_float],
+        'ofd_set_coefficients': [h, ctypes.c_int, fptr, ctypes.c_int, fptr, ctypes.c_int],
         'ofd_set_media': [h, fptr, fptr, fptr],
         'ofd_upload_field': [h, ctypes.c_int, ctypes.c_int, fptr],
         'ofd_download_field': [h, ctypes.c_int, ctypes.c_int, fptr],
@@ -76,6 +77,7 @@ def load_library():
         'ofd_set_source': [h, ctypes.c_int, ctypes.c_int, ctypes.c_int, fptr, ctypes.c_int],
         'ofd_apply_boundary_init': [h, ctypes.c_int],
         'ofd_step': [h, ctypes.c_int],
+        'ofd_step_profiled': [h, ctypes.c_int, P(ctypes.c_double), P(ctypes.c_double), P(ctypes.c_long)],
         'ofd_sync': [h],
         'ofd_get_step': [h, P(ctypes.c_long)],
         'ofd_set_step': [h, ctypes.c_long],
@@ -181,6 +183,24 @@ class Simulation(object):
             a = a.reshape(self.dims)
         return a
 
+    def set_coefficients(self, het, ks, kv):
+        ks = np.ascontiguousarray(ks, dtype=np.float32)
+        kv = np.ascontiguousarray(kv, dtype=np.float32)
+        _check(self.lib.ofd_set_coefficients(self.h, int(het), _fptr(ks), len(ks), _fptr(kv), len(kv)),
+               'ofd_set_coefficients')
+
+    def set_coefficients_from_grid(self, grid):
+        """Literal tables of the grid's generated update expressions, after
+        checking that their structure is the prebuilt one."""
+        from .templates import cuda_gen
+        tabs = cuda_gen.sweep_tables(grid)
+        key = 'so%d_%s' % (grid.order[1], 'het' if grid.read else 'const')
+        pre = cuda_gen.prebuilt_signatures().get(key)
+        if pre is None or pre['stress'] != tabs['stress'][0] or pre['velocity'] != tabs['velocity'][0]:
+            raise OFDError('the update expressions of this model (%s) do not match the prebuilt '
+                           'CUDA expressions; regenerate csrc/generated' % key)
+        self.set_coefficients(1 if grid.read else 0, tabs['stress'][1], tabs['velocity'][1])
+
     def set_media_const(self, beta, lam, mu):
         _check(self.lib.ofd_set_media_const(self.h, beta, lam, mu), 'ofd_set_media_const')
 
@@ -214,6 +234,17 @@ class Simulation(object):
 
     def step(self, n=1):
         _check(self.lib.ofd_step(self.h, int(n)), 'ofd_step')
+
+    def step_profiled(self, n):
+        """Advance n steps with CUDA events on the handle's stream; returns
+        (total ms, [stress sweep, stress ghosts, velocity sweep, velocity
+        ghosts] ms, kernel launches)."""
+        tot = ctypes.c_double()
+        cls = (ctypes.c_double * 4)()
+        nl = ctypes.c_long()
+        _check(self.lib.ofd_step_profiled(self.h, int(n), ctypes.byref(tot), cls, ctypes.byref(nl)),
+               'ofd_step_profiled')
+        return tot.value, list(cls), nl.value
 
     def sync(self):
         _check(self.lib.ofd_sync(self.h), 'ofd_sync')

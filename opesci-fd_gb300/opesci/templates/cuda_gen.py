@@ -1,0 +1,170 @@
+"""CUDA code generation for the sweep arithmetic.
+
+The stress and velocity updates are printed from the solved symbolic kernels
+(StaggeredGrid.kernel_sympy: expanded, constant-folded, media resolved) with
+the same C printer as the reference's generator (codeprinter.py:13-82), then
+turned into a device function by two substitutions:
+
+  * every floating literal becomes K[i] (i in order of appearance);
+  * every array reference f[_t][x+a][y+b][z+c] becomes A(F_f, a, b, c) and
+    every media reference m[x][y][z] becomes A.m(M_m).
+
+Term order, operator order and the arithmetic of the reference's C
+expression are therefore kept; only the literal values move to a run-time
+table.  SymPy orders the terms of these kernels by their array parts, so the
+printed structure depends on the space order and the media mode, not on dt,
+spacing or media values; each model's structure is checked against the
+signature of the generated header before its table is used.
+
+``python -m opesci.templates.cuda_gen`` (from opesci-fd_gb300/) regenerates
+csrc/generated/sweeps_gen.cuh and signatures.json for space orders 2-8 with
+constant and heterogeneous media.
+"""
+import hashlib
+import json
+import os
+import re
+from fractions import Fraction
+
+import numpy as np
+
+from ..codeprinter import ccode
+
+_LIT = re.compile(r'(?<![\w\]\.])(\d+\.\d*(?:e[+-]?\d+)?)F')
+_ARR = re.compile(r'\b(U|V|W|Txx|Tyy|Tzz|Txy|Tyz|Txz)\[_t[01]\]\[x(?: ([+-]) (\d+))?\]\[y(?: ([+-]) (\d+))?\]\[z(?: ([+-]) (\d+))?\]')
+_MED = re.compile(r'\b(lambda|mu12|mu13|mu23|mu|beta1|beta2|beta3)\[x\]\[y\]\[z\]')
+_FIELD = {'U': 'F_U', 'V': 'F_V', 'W': 'F_W', 'Txx': 'F_TXX', 'Tyy': 'F_TYY', 'Tzz': 'F_TZZ',
+          'Txy': 'F_TXY', 'Tyz': 'F_TYZ', 'Txz': 'F_TXZ'}
+_MEDIA = {'lambda': 'M_LAM', 'mu': 'M_MU', 'mu12': 'M_MU12', 'mu13': 'M_MU13', 'mu23': 'M_MU23',
+          'beta1': 'M_B1', 'beta2': 'M_B2', 'beta3': 'M_B3'}
+
+STRESS_ORDER = ['Txx', 'Tyy', 'Tzz', 'Txy', 'Tyz', 'Txz']
+VELOCITY_ORDER = ['U', 'V', 'W']
+
+
+def decimal_to_f32(text):
+    """Nearest float32 to a decimal string, ties to even — what a C compiler
+    does with the literal ``textF``."""
+    q = Fraction(text)
+    f = np.float32(float(q))
+    best = None
+    for c in (np.nextafter(f, np.float32(-np.inf)), f, np.nextafter(f, np.float32(np.inf))):
+        d = abs(Fraction(float(c)) - q)
+        key = (d, int(np.frombuffer(np.float32(c).tobytes(), dtype=np.uint32)[0]) & 1)
+        if best is None or key < best[0]:
+            best = (key, c)
+    return np.float32(best[1])
+
+
+def _sub_arrays(text):
+    def arr(m):
+        f = _FIELD[m.group(1)]
+        offs = []
+        for sgn, val in ((m.group(2), m.group(3)), (m.group(4), m.group(5)), (m.group(6), m.group(7))):
+            offs.append('0' if sgn is None else ('-' if sgn == '-' else '') + val)
+        return 'A(%s, %s)' % (f, ', '.join(offs))
+    text = _ARR.sub(arr, text)
+    text = _MED.sub(lambda m: 'A.m(%s)' % _MEDIA[m.group(1)], text)
+    return text
+
+
+def kernel_text(grid, fields):
+    """(device-expression texts, literal strings) of the update kernels of
+    ``fields`` in the grid's current switches."""
+    grid.create_const_dict()
+    exprs, lits = [], []
+    for f in fields:
+        s = ccode(grid.kernel_sympy(f))
+        parts = []
+        pos = 0
+        for m in _LIT.finditer(s):
+            parts.append(s[pos:m.start()])
+            parts.append('K[%d]' % len(lits))
+            lits.append(m.group(1))
+            pos = m.end()
+        parts.append(s[pos:])
+        body = _sub_arrays(''.join(parts))
+        if '[' in body.replace('K[', '').replace('A(', ''):
+            raise ValueError('unsupported array reference in kernel of %s: %s' % (f.label, body[:200]))
+        exprs.append(body)
+    return exprs, lits
+
+
+def signature(exprs):
+    canon = '\n'.join(re.sub(r'K\[\d+\]', 'K', e) for e in exprs)
+    return hashlib.sha1(canon.encode()).hexdigest()[:16]
+
+
+def sweep_tables(grid):
+    """Run-time coefficient tables and structure signatures of a solved
+    StaggeredGrid: {'stress': (sig, float32 array), 'velocity': (...)}."""
+    by = {f.label.name: f for f in grid.fields}
+    out = {}
+    for kind, order in (('stress', STRESS_ORDER), ('velocity', VELOCITY_ORDER)):
+        exprs, lits = kernel_text(grid, [by[n] for n in order])
+        out[kind] = (signature(exprs), np.array([decimal_to_f32(t) for t in lits], dtype=np.float32))
+    return out
+
+
+def _variant_grid(space_order, hetero):
+    from ..models import elastic_grid
+    if hetero:
+        return elastic_grid((130.0, 130.0, 130.0), (13, 13, 13), 7e-4, 7e-3, space_order=space_order,
+                            read=True, rho_file='r', vp_file='p', vs_file='s', analytic=False,
+                            free_surface=False)
+    return elastic_grid((1.0, 1.0, 1.0), (13, 13, 13), 3e-3, 3e-2, space_order=space_order,
+                        analytic=False, free_surface=False)
+
+
+def generate_headers(outdir):
+    """Write sweeps_gen.cuh and signatures.json for all prebuilt variants."""
+    os.makedirs(outdir, exist_ok=True)
+    sigs = {}
+    lines = ['// GENERATED by opesci/templates/cuda_gen.py from the symbolic kernels of',
+             '// StaggeredGrid (expanded, constant-folded, media resolved); do not edit.',
+             '// Each function evaluates the reference generator\'s C expression of the',
+             '// update with its literals taken from the table K.',
+             '#pragma once', '#include "ofd_common.cuh"', '', 'namespace ofd {', '',
+             'template <int R, int HET> struct GenSweep { static constexpr bool ok = false; };', '']
+    for so in (2, 4, 6, 8):
+        for het in (0, 1):
+            g = _variant_grid(so, het)
+            by = {f.label.name: f for f in g.fields}
+            se, sl = kernel_text(g, [by[n] for n in STRESS_ORDER])
+            ve, vl = kernel_text(g, [by[n] for n in VELOCITY_ORDER])
+            key = 'so%d_%s' % (so, 'het' if het else 'const')
+            sigs[key] = {'stress': signature(se), 'velocity': signature(ve),
+                         'nk_stress': len(sl), 'nk_velocity': len(vl)}
+            lines.append('template <> struct GenSweep<%d, %d> {' % (so // 2, het))
+            lines.append('  static constexpr bool ok = true;')
+            lines.append('  static constexpr int NK_STRESS = %d, NK_VELOCITY = %d;' % (len(sl), len(vl)))
+            lines.append('  template <typename C, class Acc>')
+            lines.append('  __device__ __forceinline__ static void stress(const Acc &A, const float *K, C out[6]) {')
+            for i, e in enumerate(se):
+                lines.append('    out[%d] = %s;' % (i, e))
+            lines.append('  }')
+            lines.append('  template <typename C, class Acc>')
+            lines.append('  __device__ __forceinline__ static void velocity(const Acc &A, const float *K, C out[3]) {')
+            for i, e in enumerate(ve):
+                lines.append('    out[%d] = %s;' % (i, e))
+            lines.append('  }')
+            lines.append('};')
+            lines.append('')
+    lines.append('}  // namespace ofd')
+    with open(os.path.join(outdir, 'sweeps_gen.cuh'), 'w') as f:
+        f.write('\n'.join(lines) + '\n')
+    with open(os.path.join(outdir, 'signatures.json'), 'w') as f:
+        json.dump(sigs, f, indent=1, sort_keys=True)
+    return sigs
+
+
+def prebuilt_signatures():
+    path = os.path.join(os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))),
+                        'csrc', 'generated', 'signatures.json')
+    with open(path) as f:
+        return json.load(f)
+
+
+if __name__ == '__main__':
+    here = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    print(generate_headers(os.path.join(here, 'csrc', 'generated')))

@@ -2,10 +2,14 @@
 against the oracle, the reference-shaped C++ program run on the CPU.
 
 Tolerance: FP32, every field within 1e-5 relative L2 of the oracle after the
-run.  The eigenmode's shear stresses are zero analytically; their computed
-values are rounding residue of cancelling velocity differences, so for those
-three fields the difference is measured relative to the norm of the whole
-stress family (Txx..Txz) instead of their own near-zero norm.
+run.  For the heterogeneous problem with a source every field is a
+propagating wave and the norm is each field's own.  The eigenmode trades its
+energy between velocities and stresses: its shear stresses are zero
+analytically (their values are rounding residue of cancelling differences)
+and at some final times the normal stresses are near zero too (sin(Omega t)
+= 0 at t = 2 for the reference's own test3d problem).  For the eigenmode each
+field's difference is therefore measured against the norm of the whole
+nine-field state, the quantity the scheme conserves.
 """
 import json
 import os
@@ -26,6 +30,7 @@ STRESS = ('Txx', 'Tyy', 'Tzz', 'Txy', 'Tyz', 'Txz')
 
 def run_eigen_gpu(g, variant=0, storage=None, steps=None):
     sim = runtime.Simulation(runtime.config_from_grid(g, kernel_variant=variant, storage=storage))
+    sim.set_coefficients_from_grid(g)
     dv = g.defined_variable
     sim.set_media_const(dv['beta'].value, dv['lambda'].value, dv['mu'].value)
     for k, v in initial_fields(g).items():
@@ -40,6 +45,7 @@ def run_eigen_gpu(g, variant=0, storage=None, steps=None):
 
 def run_problem_gpu(g, media, src, wav, variant=0, storage='f32'):
     sim = runtime.Simulation(runtime.config_from_grid(g, kernel_variant=variant, storage=storage))
+    sim.set_coefficients_from_grid(g)
     sim.set_media(*media)
     sim.set_source(src, wav)
     sim.step(g.ntsteps.value)
@@ -49,12 +55,14 @@ def run_problem_gpu(g, media, src, wav, variant=0, storage='f32'):
     return out
 
 
-def rel_errors(got, ref, shear_by_family=False):
-    fam = np.sqrt(sum(np.linalg.norm(ref[f].astype(np.float64)) ** 2 for f in STRESS))
+def rel_errors(got, ref, state_norm=False):
+    """Per-field relative L2 differences; with state_norm the denominator is
+    the norm of the whole nine-field state instead of the field's own."""
+    state = np.sqrt(sum(np.linalg.norm(ref[f].astype(np.float64)) ** 2 for f in runtime.FIELDS))
     out = {}
     for f in runtime.FIELDS:
         a, b = got[f].astype(np.float64), ref[f].astype(np.float64)
-        den = fam if (shear_by_family and f in SHEAR) else np.linalg.norm(b)
+        den = state if state_norm else np.linalg.norm(b)
         out[f] = float(np.linalg.norm(a - b) / max(den, 1e-300))
     return out
 
@@ -64,7 +72,7 @@ def test_eigenwave_matches_oracle(tmp_path, so, n, steps):
     g = eigenwave_grid(grid_size=(n, n, n), ntsteps=steps, space_order=so)
     got = run_eigen_gpu(g)
     ref = orun.run(g, str(tmp_path))
-    errs = rel_errors(got, ref['fields'], shear_by_family=True)
+    errs = rel_errors(got, ref['fields'], state_norm=True)
     assert max(errs.values()) < TOL, errs
     # analytic-solution error norms, FP64 on both sides
     for f in g.fields:
@@ -73,7 +81,7 @@ def test_eigenwave_matches_oracle(tmp_path, so, n, steps):
         assert abs(e_gpu - ref['l2_fp64'][name]) <= 1e-4 * ref['l2_fp64'][name] + 1e-12, name
 
 
-@pytest.mark.parametrize('so', [4, 8])
+@pytest.mark.parametrize('so', [2, 4, 6, 8])
 def test_heterogeneous_source_matches_oracle(tmp_path, so):
     files = {k: str(tmp_path / (k + '.raw')) for k in ('rho', 'vp', 'vs')}
     g, media, src, wav = layered_problem(40, space_order=so, ntsteps=120, seed=11, media_files=files)
@@ -82,6 +90,12 @@ def test_heterogeneous_source_matches_oracle(tmp_path, so):
     errs = rel_errors(got, ref['fields'])
     assert max(errs.values()) < TOL, errs
     assert np.abs(got['Txx']).max() > 0
+    if so != 4:
+        # Robertsson ghosts are exact zeros and mirrors exact negations, and
+        # the sweeps evaluate the reference's own expression without
+        # contraction: the run is bit-identical to the reference's C++
+        for f in runtime.FIELDS:
+            assert np.array_equal(got[f], ref['fields'][f]), f
 
 
 def test_legacy_gpu_reproduces_reference_test3d(tmp_path):
@@ -94,7 +108,7 @@ def test_legacy_gpu_reproduces_reference_test3d(tmp_path):
     g = eigenwave_grid(grid_size=(100, 100, 100), dt=0.002, ntsteps=1000, legacy=True)
     got = run_eigen_gpu(g)
     ref = orun.run(g, str(tmp_path), legacy=True)
-    errs = rel_errors(got, ref['fields'], shear_by_family=True)
+    errs = rel_errors(got, ref['fields'], state_norm=True)
     assert max(errs.values()) < TOL, errs
     for f in g.fields:
         name = f.label.name
@@ -103,12 +117,24 @@ def test_legacy_gpu_reproduces_reference_test3d(tmp_path):
         assert abs(e - gold['l2'][name]) < 2e-3 * gold['l2'][name], (name, e, gold['l2'][name])
 
 
-def test_plain_and_best_kernels_agree():
-    g, media, src, wav = layered_problem(72, space_order=4, ntsteps=40, seed=5)
+@pytest.mark.parametrize('so,n', [(2, 70), (4, 72), (4, 101), (6, 66)])
+def test_tiled_and_plain_kernels_identical(so, n):
+    """The TMA-tiled sweeps evaluate the same generated expression as the
+    plain sweeps: results are bit-identical, also with partial tiles."""
+    g, media, src, wav = layered_problem(n, space_order=so, ntsteps=24, seed=5)
     a = run_problem_gpu(g, media, src, wav, variant=0)
     b = run_problem_gpu(g, media, src, wav, variant=1)
-    errs = rel_errors(a, b)
-    assert max(errs.values()) < 1e-6, errs
+    for f in runtime.FIELDS:
+        assert np.array_equal(a[f], b[f]), f
+    assert np.abs(a['Txx']).max() > 0
+
+
+def test_tiled_constant_media_identical():
+    g = eigenwave_grid(grid_size=(80, 80, 80), ntsteps=12, space_order=4)
+    a = run_eigen_gpu(g, variant=0)
+    b = run_eigen_gpu(g, variant=1)
+    for f in runtime.FIELDS:
+        assert np.array_equal(a[f], b[f]), f
 
 
 def test_steps_are_resumable():
@@ -117,6 +143,7 @@ def test_steps_are_resumable():
     g, media, src, wav = layered_problem(32, space_order=4, ntsteps=30, seed=2)
     a = run_problem_gpu(g, media, src, wav)
     sim = runtime.Simulation(runtime.config_from_grid(g))
+    sim.set_coefficients_from_grid(g)
     sim.set_media(*media)
     sim.set_source(src, wav)
     for n in (7, 13, 10):
@@ -132,6 +159,7 @@ def test_error_paths_leave_context_usable():
     from opesci.runtime import OFDError
     g, media, src, wav = layered_problem(24, space_order=4, ntsteps=5, seed=1)
     sim = runtime.Simulation(runtime.config_from_grid(g))
+    sim.set_coefficients_from_grid(g)
     with pytest.raises(OFDError, match='outside'):
         sim.set_source((10000, 1, 1), wav)
     with pytest.raises(OFDError, match='bad field'):
