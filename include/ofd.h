@@ -137,6 +137,23 @@ typedef struct ofd_field_view {
 } ofd_field_view;
 int ofd_field_view_get(ofd_handle *h, int field, int level, ofd_field_view *out);
 
+/* Allocation-free FP64 sum of squares of one field (no counterpart in the
+ * reference).  For callers that cannot allocate device memory: code running
+ * during CUDA graph capture, plugins confined to another framework's memory
+ * pool, and latency-bound serving loops that must not synchronise on the
+ * allocator.  field: device array in the reference layout
+ * float[dims[0]][dims[1]][dims[2]]; the sum covers the interior
+ * [margin, dims-margin)^3; *out (device memory) receives the sum.  Work is
+ * queued on stream (a cudaStream_t, NULL for the default stream).  Partial
+ * sums live in a fixed 32 KB device array of the library, one entry per x
+ * plane: at most 4096 interior planes, larger grids are rejected.  The first
+ * call on each device looks up that array's device address; make it before
+ * any stream capture.  All calls share the array: calls whose work overlaps
+ * on the GPU race and must be serialised.  ofd_noalloc_last_error() describes
+ * the last failure of this entry point on the calling thread. */
+int ofd_sumsq_field_noalloc(const float *field, const int dims[3], int margin, double *out, void *stream);
+const char *ofd_noalloc_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif
