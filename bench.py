@@ -246,13 +246,21 @@ def main():
 
     e2e = None
     if not args.no_e2e:
-        # the C-ABI job as a user runs it: host media in, K steps, 9 host fields out
-        host_fields = [np.empty(sim.dims, dtype=np.float32) for _ in range(9)]
+        # the C-ABI job as a user runs it: media from pinned host memory in,
+        # K steps, the 9 final fields out to pinned host memory
+        import torch
+        pin = lambda: torch.empty(sim.dims, dtype=torch.float32, pin_memory=True).numpy()  # noqa: E731
+        host_media = []
+        for arr in media:
+            hb = pin()
+            hb[...] = arr
+            host_media.append(hb)
+        host_fields = [pin() for _ in range(9)]
         sim.sync()
         t0 = time.perf_counter()
         sim.zero()
         sim.steps = 0
-        sim.set_media(*media)
+        sim.set_media(*host_media)
         sim.set_source(src, wav)
         sim.step(args.steps)
         lvl = args.steps % 2

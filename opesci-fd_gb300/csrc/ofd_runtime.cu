@@ -38,16 +38,18 @@ static int fail(int code, const char *fmt, ...) {
 // rounded to float like the reference's C expressions, on the whole padded
 // grid with upper neighbours clamped at the last index.
 __global__ void media_base_kernel(const float *rho, const float *vp, const float *vs, float *beta,
-                                  float *lam, float *mu, long n) {
+                                  float *lam, float *mu, double *inv_mu, long n) {
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
     const double r = rho[i], p = vp[i], s = vs[i];
     beta[i] = (float)(1.0 / r);
     lam[i] = (float)(r * (p * p - 2.0 * (s * s)));
-    mu[i] = (float)(r * (s * s));
+    const float m = (float)(r * (s * s));
+    mu[i] = m;
+    inv_mu[i] = 1.0 / (double)m;   // the 1.0/mu of the harmonic means, computed once per point
   }
 }
 
-__global__ void media_avg_kernel(const float *beta, const float *lam, const float *mu, Geom g,
+__global__ void media_avg_kernel(const float *beta, const float *lam, const float *mu, const double *im, Geom g,
                                  float *o_lam, float *o_mu, float *o_mu12, float *o_mu13,
                                  float *o_mu23, float *o_b1, float *o_b2, float *o_b3) {
   const long n = (long)g.n1 * g.n2 * g.n3;
@@ -65,13 +67,10 @@ __global__ void media_avg_kernel(const float *beta, const float *lam, const floa
     o_b1[o] = (b0 + beta[D(x1, y, z)]) * 0.5f;
     o_b2[o] = (b0 + beta[D(x, y1, z)]) * 0.5f;
     o_b3[o] = (b0 + beta[D(x, y, z1)]) * 0.5f;
-    const double m0 = 1.0 / (double)mu[i];
-    o_mu12[o] = (float)(1.0 / (0.25 * (m0 + 1.0 / (double)mu[D(x1, y, z)] + 1.0 / (double)mu[D(x, y1, z)] +
-                                       1.0 / (double)mu[D(x1, y1, z)])));
-    o_mu13[o] = (float)(1.0 / (0.25 * (m0 + 1.0 / (double)mu[D(x1, y, z)] + 1.0 / (double)mu[D(x, y, z1)] +
-                                       1.0 / (double)mu[D(x1, y, z1)])));
-    o_mu23[o] = (float)(1.0 / (0.25 * (m0 + 1.0 / (double)mu[D(x, y1, z)] + 1.0 / (double)mu[D(x, y, z1)] +
-                                       1.0 / (double)mu[D(x, y1, z1)])));
+    const double m0 = im[i];
+    o_mu12[o] = (float)(1.0 / (0.25 * (m0 + im[D(x1, y, z)] + im[D(x, y1, z)] + im[D(x1, y1, z)])));
+    o_mu13[o] = (float)(1.0 / (0.25 * (m0 + im[D(x1, y, z)] + im[D(x, y, z1)] + im[D(x1, y, z1)])));
+    o_mu23[o] = (float)(1.0 / (0.25 * (m0 + im[D(x, y1, z)] + im[D(x, y, z1)] + im[D(x, y1, z1)])));
   }
 }
 
@@ -365,12 +364,15 @@ int ofd_set_media(ofd_handle *h, const float *rho, const float *vp, const float 
   const Geom &g = h->s.g;
   const long n = (long)g.n1 * g.n2 * g.n3;
   float *tmp = nullptr;
-  OFD_CUDA(cudaMallocAsync((void **)&tmp, sizeof(float) * n * 6, h->stream));
+  // six float arrays then one double array
+  OFD_CUDA(cudaMallocAsync((void **)&tmp, sizeof(float) * n * 6 + sizeof(double) * n + 256, h->stream));
+  double *inv_mu = (double *)(((uintptr_t)(tmp + 6 * n) + 255) & ~(uintptr_t)255);
   OFD_CUDA(cudaMemcpyAsync(tmp, rho, sizeof(float) * n, cudaMemcpyHostToDevice, h->stream));
   OFD_CUDA(cudaMemcpyAsync(tmp + n, vp, sizeof(float) * n, cudaMemcpyHostToDevice, h->stream));
   OFD_CUDA(cudaMemcpyAsync(tmp + 2 * n, vs, sizeof(float) * n, cudaMemcpyHostToDevice, h->stream));
-  media_base_kernel<<<1216, 256, 0, h->stream>>>(tmp, tmp + n, tmp + 2 * n, tmp + 3 * n, tmp + 4 * n, tmp + 5 * n, n);
-  media_avg_kernel<<<1216, 256, 0, h->stream>>>(tmp + 3 * n, tmp + 4 * n, tmp + 5 * n, g, h->s.media[M_LAM],
+  media_base_kernel<<<1216, 256, 0, h->stream>>>(tmp, tmp + n, tmp + 2 * n, tmp + 3 * n, tmp + 4 * n, tmp + 5 * n,
+                                                 inv_mu, n);
+  media_avg_kernel<<<1216, 256, 0, h->stream>>>(tmp + 3 * n, tmp + 4 * n, tmp + 5 * n, inv_mu, g, h->s.media[M_LAM],
                                                 h->s.media[M_MU], h->s.media[M_MU12], h->s.media[M_MU13],
                                                 h->s.media[M_MU23], h->s.media[M_B1], h->s.media[M_B2],
                                                 h->s.media[M_B3]);

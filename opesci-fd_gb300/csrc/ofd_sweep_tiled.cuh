@@ -24,8 +24,9 @@
 namespace ofd {
 
 constexpr int TZ = 64;          // tile width along z (two 32-lane passes)
-constexpr int TY = 8;           // tile height along y (one warp per row)
-constexpr int TILED_THREADS = TZ / 2 * TY;   // 256: warp w -> row w, lane l -> z = l, l+32
+// tile height along y (one warp per row).  Eight rows let two CTAs share an SM
+// (measured faster than one CTA of sixteen rows, despite the extra halo rows)
+__host__ __device__ constexpr int tile_rows(int) { return 8; }
 
 template <typename S> struct ZHalo { static constexpr int v = (int)(16 / sizeof(S)) >= 4 ? (int)(16 / sizeof(S)) : 4; };
 
@@ -49,15 +50,15 @@ struct TiledCtx {
 inline void tiled_boxes(int R, int esize, int *hw, int *hh, int *pw, int *ph) {
   const int zh = (16 / esize) >= 4 ? 16 / esize : 4;
   *hw = TZ + 2 * zh;
-  *hh = TY + 2 * R;
+  *hh = tile_rows(R) + 2 * R;
   *pw = TZ;
-  *ph = TY;
+  *ph = tile_rows(R);
 }
 
 struct TiledParams {
-  CUtensorMap hmap[6];     // halo arrays in order of hfield[]
-  CUtensorMap pmap[6];     // point field arrays in order of pfield[]
-  CUtensorMap mmap[5];     // media arrays in order of mfield[]
+  CUtensorMap hmap[6];     // halo boxes: x-window arrays, then plane-halo arrays
+  CUtensorMap pmap[6];     // point boxes of field arrays
+  CUtensorMap mmap[5];     // point boxes of media arrays
   int *err;                // error word (bounded waits)
   int zcoord0;             // TMA x coordinate of z = m (z0 + m)
   int chunk;               // planes per CTA along x
@@ -100,141 +101,165 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, u
 
 __host__ __device__ constexpr int round128(int b) { return (b + 127) / 128 * 128; }
 
-// Compile-time description of one sweep.
+// Compile-time description of one sweep.  Roles of the arrays read:
+//   X  ("x-window"): read at x offsets and with y/z neighbours -> ring of NSH
+//      halo boxes (stress: U V W; velocity: Txx Txy Txz)
+//   H  ("plane halo"): y/z neighbours at the current plane only -> ring of NSC
+//      halo boxes (velocity: Tyy Tyz Tzz)
+//   P  (point): the value at the point (stress: the six stresses at t0;
+//      velocity: U V W at t0) and the media arrays -> ring of NSC point boxes
 template <int R, typename S, int HET, bool STRESS>
 struct TiledCfg {
+  static constexpr int TY = tile_rows(R);
+  static constexpr int THREADS = 32 * TY;
   static constexpr int ZH = ZHalo<S>::v;                  // z halo, rounded to 16 B
   static constexpr int HW = TZ + 2 * ZH;                   // halo box width
   static constexpr int HH = TY + 2 * R;                    // halo box height
-  static constexpr int NHF = STRESS ? 3 : 6;               // halo arrays
+  static constexpr int NXF = 3;                            // x-window arrays
+  static constexpr int NH0 = STRESS ? 0 : 3;               // plane-halo arrays
   static constexpr int NPF = STRESS ? 6 : 3;               // point field arrays
   static constexpr int NMF = HET ? (STRESS ? 5 : 3) : 0;   // point media arrays
   static constexpr int PF = 1;                             // planes prefetched ahead
-  static constexpr int NSH = 2 * R + 1 + PF;               // halo ring depth
-  static constexpr int NSC = 1 + PF;                       // point ring depth
+  static constexpr int NSH = 2 * R + 1 + PF;               // x-window ring depth
+  static constexpr int NSC = 1 + PF;                       // plane ring depth
   static constexpr int HBOX = HW * HH * (int)sizeof(S);
   static constexpr int HSLOT = round128(HBOX);
   static constexpr int PBOX = TZ * TY * (int)sizeof(S);
+  static constexpr int PSLOT = round128(PBOX);
   static constexpr int MBOX = TZ * TY * 4;
-  static constexpr int HRING = NSH * NHF * HSLOT;
-  static constexpr int PRING = NSC * NPF * round128(PBOX);
-  static constexpr int MRING = NSC * (NMF > 0 ? NMF : 1) * round128(MBOX);
+  static constexpr int MSLOT = round128(MBOX);
+  // one x-window ring stage holds NXF halo boxes; one plane ring stage holds
+  // NH0 halo boxes, NPF point boxes and NMF media boxes
+  static constexpr int XSTAGE = NXF * HSLOT;
+  static constexpr int CSTAGE = NH0 * HSLOT + NPF * PSLOT + NMF * MSLOT;
+  static constexpr int XRING = NSH * XSTAGE;
+  static constexpr int CRING = NSC * CSTAGE;
   static constexpr int BARS = (NSH + NSC) * 8;
-  static constexpr int SMEM = HRING + PRING + MRING + round128(BARS) + 128;  // +128: base alignment
-  // field id -> slot in the halo / point lists
-  __host__ __device__ static constexpr int hidx(int f) { return STRESS ? (f - F_U) : (f - F_TXX); }
-  __host__ __device__ static constexpr int pidx(int f) { return STRESS ? (f - F_TXX) : (f - F_U); }
-  __host__ __device__ static constexpr bool is_halo(int f) { return STRESS ? (f < F_TXX) : (f >= F_TXX); }
-  __host__ __device__ static constexpr int midx(int m) {
-    return STRESS ? (m - M_LAM) : (m - M_B1);
+  static constexpr int SMEM = XRING + CRING + round128(BARS) + 128;  // +128: base alignment
+  static constexpr unsigned XBYTES = NXF * HBOX;
+  static constexpr unsigned CBYTES = NH0 * HBOX + NPF * PBOX + NMF * MBOX;
+  // role and index of a field id
+  __host__ __device__ static constexpr int role(int f) {   // 0 X, 1 H, 2 P
+    return STRESS ? (f < F_TXX ? 0 : 2)
+                  : (f < F_TXX ? 2 : ((f == F_TXX || f == F_TXY || f == F_TXZ) ? 0 : 1));
   }
+  __host__ __device__ static constexpr int xidx(int f) {
+    return STRESS ? (f - F_U) : (f == F_TXX ? 0 : (f == F_TXY ? 1 : 2));
+  }
+  __host__ __device__ static constexpr int h0idx(int f) { return f == F_TYY ? 0 : (f == F_TYZ ? 1 : 2); }
+  __host__ __device__ static constexpr int pidx(int f) { return STRESS ? (f - F_TXX) : (f - F_U); }
+  __host__ __device__ static constexpr int midx(int m) { return STRESS ? (m - M_LAM) : (m - M_B1); }
+  // byte offset of a box inside a plane-ring stage
+  __host__ __device__ static constexpr int h0off(int i) { return i * HSLOT; }
+  __host__ __device__ static constexpr int poff(int i) { return NH0 * HSLOT + i * PSLOT; }
+  __host__ __device__ static constexpr int moff(int i) { return NH0 * HSLOT + NPF * PSLOT + i * MSLOT; }
 };
 
+// Accessor of the generated expressions: xs[k] is the x-window stage of plane
+// x + k - R, cs the plane-ring stage of plane x; hpos/ppos the thread's
+// element offset inside a halo box / point box.  Every read is one shared
+// load at a compile-time offset from one of these bases.
 template <int R, typename S, int HET, bool STRESS>
 struct TiledAcc {
   typedef TiledCfg<R, S, HET, STRESS> G;
   typedef typename Storage<S>::C C;
-  const S *hring;     // halo ring base
-  const S *pring;
-  const float *mring;
+  const unsigned char *xs[2 * R + 1];
+  const unsigned char *cs;
   const float *inv;
-  int x, hq0;         // current plane, halo-ring plane origin (plane of q = 0)
-  int pq0;
-  int yl, zl;         // thread row / column in the tile
+  int hpos, ppos;
   __device__ __forceinline__ C operator()(int f, int dx, int dy, int dz) const {
-    if (G::is_halo(f)) {
-      const int q = x + dx - hq0;
-      const int slot = q % G::NSH;
-      const S *b = (const S *)((const char *)hring + (slot * G::NHF + G::hidx(f)) * G::HSLOT);
-      return (C)Storage<S>::load(b[(yl + R + dy) * G::HW + (zl + G::ZH + dz)], inv[f]);
+    const int off = dy * G::HW + dz;
+    if (G::role(f) == 0) {
+      const S *b = (const S *)(xs[dx + R] + G::xidx(f) * G::HSLOT);
+      return (C)Storage<S>::load(b[hpos + off], inv[f]);
     }
-    const int q = x - pq0;
-    const int slot = q % G::NSC;
-    const S *b = (const S *)((const char *)pring + (slot * G::NPF + G::pidx(f)) * round128(G::PBOX));
-    return (C)Storage<S>::load(b[yl * TZ + zl], inv[f]);
+    if (G::role(f) == 1) {
+      const S *b = (const S *)(cs + G::h0off(G::h0idx(f)));
+      return (C)Storage<S>::load(b[hpos + off], inv[f]);
+    }
+    const S *b = (const S *)(cs + G::poff(G::pidx(f)));
+    return (C)Storage<S>::load(b[ppos], inv[f]);
   }
   __device__ __forceinline__ C m(int i) const {
-    const int q = x - pq0;
-    const int slot = q % G::NSC;
-    const float *b = (const float *)((const char *)mring + (slot * (G::NMF > 0 ? G::NMF : 1) + G::midx(i)) * round128(G::MBOX));
-    return (C)b[yl * TZ + zl];
+    const float *b = (const float *)(cs + G::moff(G::midx(i)));
+    return (C)b[ppos];
   }
 };
 
+template <int R> struct TiledThreads { static constexpr int v = 32 * tile_rows(R); };
+
 template <int R, typename S, int HET, bool STRESS>
-__global__ void __launch_bounds__(TILED_THREADS)
+__global__ void __launch_bounds__(TiledThreads<R>::v)
 sweep_tiled(const __grid_constant__ SweepArgs<S> a, const __grid_constant__ TiledParams p) {
   typedef TiledCfg<R, S, HET, STRESS> G;
   typedef typename Storage<S>::C C;
   extern __shared__ unsigned char smem_raw[];
   unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127);
-  S *hring = (S *)smem;
-  S *pring = (S *)(smem + G::HRING);
-  float *mring = (float *)(smem + G::HRING + G::PRING);
-  uint64_t *hbar = (uint64_t *)(smem + G::HRING + G::PRING + G::MRING);
-  uint64_t *pbar = hbar + G::NSH;
+  unsigned char *xring = smem;
+  unsigned char *cring = smem + G::XRING;
+  uint64_t *xbar = (uint64_t *)(smem + G::XRING + G::CRING);
+  uint64_t *cbar = xbar + G::NSH;
   __shared__ int abort_flag;
 
   const Geom &g = a.g;
+  constexpr int TY = G::TY;
   const int tz = blockIdx.x % p.ntz, ty = blockIdx.x / p.ntz;
   const int z0 = g.m + tz * TZ, y0 = g.m + ty * TY;
   const int xb = g.m + blockIdx.y * p.chunk;
   const int xe = min(xb + p.chunk, g.n1 - g.m);
   if (xb >= xe) return;
-  const int hq0 = xb - R;          // plane of halo q = 0
-  const int hlast = xe - 1 + R;    // last halo plane needed
+  const int hq0 = xb - R;          // plane of x-window ring q = 0
+  const int hlast = xe - 1 + R;    // last x-window plane needed
   const int tid = threadIdx.x;
   const int zc = p.zcoord0 + (z0 - g.m);
 
-  auto issue_halo = [&](int plane) {
-    const int q = plane - hq0;
-    const int slot = q % G::NSH;
-    uint64_t *bar = &hbar[slot];
-    mbar_expect_tx(bar, G::NHF * G::HBOX);
+  auto issue_x = [&](int plane) {
+    const int slot = (plane - hq0) % G::NSH;
+    uint64_t *bar = &xbar[slot];
+    mbar_expect_tx(bar, G::XBYTES);
+    unsigned char *st = xring + slot * G::XSTAGE;
 #pragma unroll
-    for (int i = 0; i < G::NHF; ++i)
-      tma_load_3d((char *)hring + (slot * G::NHF + i) * G::HSLOT, &p.hmap[i], bar, zc - G::ZH, y0 - R, plane);
+    for (int i = 0; i < G::NXF; ++i) tma_load_3d(st + i * G::HSLOT, &p.hmap[i], bar, zc - G::ZH, y0 - R, plane);
   };
-  auto issue_point = [&](int plane) {
-    const int q = plane - xb;
-    const int slot = q % G::NSC;
-    uint64_t *bar = &pbar[slot];
-    mbar_expect_tx(bar, G::NPF * G::PBOX + G::NMF * G::MBOX);
+  auto issue_c = [&](int plane) {
+    const int slot = (plane - xb) % G::NSC;
+    uint64_t *bar = &cbar[slot];
+    mbar_expect_tx(bar, G::CBYTES);
+    unsigned char *st = cring + slot * G::CSTAGE;
 #pragma unroll
-    for (int i = 0; i < G::NPF; ++i)
-      tma_load_3d((char *)pring + (slot * G::NPF + i) * round128(G::PBOX), &p.pmap[i], bar, zc, y0, plane);
+    for (int i = 0; i < G::NH0; ++i) tma_load_3d(st + G::h0off(i), &p.hmap[G::NXF + i], bar, zc - G::ZH, y0 - R, plane);
 #pragma unroll
-    for (int i = 0; i < G::NMF; ++i)
-      tma_load_3d((char *)mring + (slot * G::NMF + i) * round128(G::MBOX), &p.mmap[i], bar, zc, y0, plane);
+    for (int i = 0; i < G::NPF; ++i) tma_load_3d(st + G::poff(i), &p.pmap[i], bar, zc, y0, plane);
+#pragma unroll
+    for (int i = 0; i < G::NMF; ++i) tma_load_3d(st + G::moff(i), &p.mmap[i], bar, zc, y0, plane);
   };
 
   int hissued = hq0 - 1, pissued = xb - 1;   // last plane issued (thread 0)
   if (tid == 0) {
     abort_flag = 0;
-    for (int i = 0; i < G::NSH; ++i) mbar_init(&hbar[i], 1);
-    for (int i = 0; i < G::NSC; ++i) mbar_init(&pbar[i], 1);
+    for (int i = 0; i < G::NSH; ++i) mbar_init(&xbar[i], 1);
+    for (int i = 0; i < G::NSC; ++i) mbar_init(&cbar[i], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    for (int pl = hq0; pl <= hlast && pl < hq0 + G::NSH; ++pl) { issue_halo(pl); hissued = pl; }
-    for (int pl = xb; pl < xe && pl < xb + G::NSC; ++pl) { issue_point(pl); pissued = pl; }
+    for (int pl = hq0; pl <= hlast && pl < hq0 + G::NSH; ++pl) { issue_x(pl); hissued = pl; }
+    for (int pl = xb; pl < xe && pl < xb + G::NSC; ++pl) { issue_c(pl); pissued = pl; }
   }
   __syncthreads();
 
   const int yl = tid >> 5, lane = tid & 31;
   const int y = y0 + yl;
-  int hwaited = hq0 - 1;   // last halo plane waited for
-  int pwaited = xb - 1;    // last point plane waited for
+  int hwaited = hq0 - 1;   // last x-window plane waited for
+  int pwaited = xb - 1;    // last plane-ring plane waited for
   bool ok = true;
   for (int x = xb; x < xe && ok; ++x) {
-    // halo planes up to x + R, point plane x
     for (int pl = hwaited + 1; pl <= x + R && ok; ++pl) {
       const int q = pl - hq0;
-      if (!mbar_wait(&hbar[q % G::NSH], (unsigned)((q / G::NSH) & 1))) ok = false;
+      if (!mbar_wait(&xbar[q % G::NSH], (unsigned)((q / G::NSH) & 1))) ok = false;
       else hwaited = pl;
     }
     if (ok) {
       const int q = x - xb;
-      if (!mbar_wait(&pbar[q % G::NSC], (unsigned)((q / G::NSC) & 1))) ok = false;
+      if (!mbar_wait(&cbar[q % G::NSC], (unsigned)((q / G::NSC) & 1))) ok = false;
       else pwaited = x;
     }
     if (!ok) {
@@ -243,11 +268,17 @@ sweep_tiled(const __grid_constant__ SweepArgs<S> a, const __grid_constant__ Tile
     }
     __syncthreads();
     if (abort_flag) break;
+    TiledAcc<R, S, HET, STRESS> A;
+#pragma unroll
+    for (int k = 0; k < 2 * R + 1; ++k) A.xs[k] = xring + ((x + k - R - hq0) % G::NSH) * G::XSTAGE;
+    A.cs = cring + ((x - xb) % G::NSC) * G::CSTAGE;
+    A.inv = a.inv;
 #pragma unroll
     for (int half = 0; half < 2; ++half) {
       const int zl = lane + 32 * half;
       const int z = z0 + zl;
-      TiledAcc<R, S, HET, STRESS> A{hring, pring, mring, a.inv, x, hq0, xb, yl, zl};
+      A.hpos = (yl + R) * G::HW + zl + G::ZH;
+      A.ppos = yl * TZ + zl;
       const long o = (long)x * g.plane + (long)y * g.P + z;
       const bool inside = (z < g.n3 - g.m) && (y < g.n2 - g.m);
       if (STRESS) {
@@ -266,24 +297,24 @@ sweep_tiled(const __grid_constant__ SweepArgs<S> a, const __grid_constant__ Tile
         }
       }
     }
-    __syncthreads();   // ring slots of plane x - R (halo) and x (point) are free
+    __syncthreads();   // stages of plane x - R (x-window) and x (plane ring) are free
     if (tid == 0) {
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       const int nh = x - R + G::NSH;
-      if (nh <= hlast) { issue_halo(nh); hissued = nh; }
+      if (nh <= hlast) { issue_x(nh); hissued = nh; }
       const int np = x + G::NSC;
-      if (np < xe) { issue_point(np); pissued = np; }
+      if (np < xe) { issue_c(np); pissued = np; }
     }
   }
   if (abort_flag && tid == 0) {
     // drain the loads this CTA issued and has not seen complete (bounded)
     for (int pl = hwaited + 1; pl <= hissued; ++pl) {
       const int q = pl - hq0;
-      mbar_wait(&hbar[q % G::NSH], (unsigned)((q / G::NSH) & 1));
+      mbar_wait(&xbar[q % G::NSH], (unsigned)((q / G::NSH) & 1));
     }
     for (int pl = pwaited + 1; pl <= pissued; ++pl) {
       const int q = pl - xb;
-      mbar_wait(&pbar[q % G::NSC], (unsigned)((q / G::NSC) & 1));
+      mbar_wait(&cbar[q % G::NSC], (unsigned)((q / G::NSC) & 1));
     }
   }
 }
@@ -298,7 +329,7 @@ static bool tiled_fits() {
 template <int R, typename S>
 bool tiled_supported(const Geom &g) {
   // the tiled path needs at least one full tile of interior along y and z
-  if (g.n3 - 2 * g.m < TZ / 2 || g.n2 - 2 * g.m < TY) return false;
+  if (g.n3 - 2 * g.m < TZ / 2 || g.n2 - 2 * g.m < tile_rows(R)) return false;
   return tiled_fits<R, S, 1, true>() && tiled_fits<R, S, 1, false>() && tiled_fits<R, S, 0, true>() &&
          tiled_fits<R, S, 0, false>();
 }
@@ -315,7 +346,9 @@ void launch_tiled(const SweepArgs<S> &a, const TiledCtx &ctx, int t0, cudaStream
     for (int i = 0; i < 6; ++i) p.pmap[i] = mp->point[F_TXX + i][t0];
     for (int i = 0; i < 5; ++i) p.mmap[i] = mp->media[M_LAM + i];
   } else {
-    for (int i = 0; i < 6; ++i) p.hmap[i] = mp->halo[F_TXX + i][t1];
+    // x-window arrays first (Txx Txy Txz), then plane-halo arrays (Tyy Tyz Tzz)
+    const int order[6] = {F_TXX, F_TXY, F_TXZ, F_TYY, F_TYZ, F_TZZ};
+    for (int i = 0; i < 6; ++i) p.hmap[i] = mp->halo[order[i]][t1];
     for (int i = 0; i < 3; ++i) p.pmap[i] = mp->point[F_U + i][t0];
     for (int i = 0; i < 3; ++i) p.mmap[i] = mp->media[M_B1 + i];
   }
@@ -323,7 +356,7 @@ void launch_tiled(const SweepArgs<S> &a, const TiledCtx &ctx, int t0, cudaStream
   p.zcoord0 = ctx.z0 + g.m;
   const int nx = g.n1 - 2 * g.m, ny = g.n2 - 2 * g.m, nz = g.n3 - 2 * g.m;
   p.ntz = (nz + TZ - 1) / TZ;
-  p.nty = (ny + TY - 1) / TY;
+  p.nty = (ny + G::TY - 1) / G::TY;
   const long tiles = (long)p.ntz * p.nty;
   // enough CTAs for ~8 waves of 152 SMs at the resident count, chunks >= 16 planes
   const int per_sm = (227 * 1024) / (G::SMEM + 1024) > 0 ? (227 * 1024) / (G::SMEM + 1024) : 1;
@@ -335,7 +368,7 @@ void launch_tiled(const SweepArgs<S> &a, const TiledCtx &ctx, int t0, cudaStream
   chunks = (nx + p.chunk - 1) / p.chunk;
   auto kern = sweep_tiled<R, S, HET, STRESS>;
   cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM);
-  kern<<<dim3((unsigned)tiles, (unsigned)chunks), TILED_THREADS, G::SMEM, st>>>(a, p);
+  kern<<<dim3((unsigned)tiles, (unsigned)chunks), G::THREADS, G::SMEM, st>>>(a, p);
 }
 
 template <int R, typename S, int HET>
