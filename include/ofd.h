@@ -123,6 +123,9 @@ int ofd_set_step(ofd_handle *h, long steps);
 
 /* FP64 sum of squares of each field over the interior [m, dim-m)^3 of a level. */
 int ofd_field_sumsq(ofd_handle *h, int level, double out[9]);
+/* Largest magnitude of each field over the interior of a level (no
+ * counterpart in the reference: used to choose 16-bit storage scales). */
+int ofd_field_absmax(ofd_handle *h, int level, double out[9]);
 
 /* Stream of the handle (cudaStream_t) for callers that interleave work. */
 void *ofd_stream(ofd_handle *h);

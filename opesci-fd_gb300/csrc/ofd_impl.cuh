@@ -49,6 +49,7 @@ struct Backend {
   virtual void to_padded(const DevState &s, const float *dense, int f, int level, cudaStream_t st) = 0;
   virtual void from_padded(const DevState &s, float *dense, int f, int level, cudaStream_t st) = 0;
   virtual void sumsq(const DevState &s, int level, double *d_out9, cudaStream_t st) = 0;
+  virtual void absmax(const DevState &s, int level, double *d_out9, cudaStream_t st) = 0;
   // literal-table sizes of the generated expressions for media mode het
   virtual int table_size(int het, int stress) const = 0;
 };
@@ -111,6 +112,44 @@ __global__ void sumsq_partial(DevState s, int level, double *partial) {
     __syncthreads();
   }
   if (threadIdx.x == 0) partial[f * gridDim.x + blockIdx.x] = sh[0];
+}
+
+// Largest magnitude of each field over the interior of a level (storage
+// scaling removed), for choosing 16-bit storage scales.
+template <typename S>
+__global__ void absmax_partial(DevState s, int level, double *partial) {
+  const Geom g = s.g;
+  const int f = blockIdx.y;
+  const S *p = (const S *)s.field[f] + (long)level * g.level;
+  const long nx = g.n1 - 2 * g.m, ny = g.n2 - 2 * g.m, nz = g.n3 - 2 * g.m;
+  const long n = nx * ny * nz;
+  const float inv = 1.f / s.scale[f];
+  double acc = 0;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const int z = (int)(i % nz) + g.m;
+    const long r = i / nz;
+    const int y = (int)(r % ny) + g.m;
+    const int x = (int)(r / ny) + g.m;
+    const double v = fabs((double)Storage<S>::load(p[(long)x * g.plane + (long)y * g.P + z], inv));
+    acc = v > acc ? v : acc;
+  }
+  __shared__ double sh[256];
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sh[threadIdx.x] = sh[threadIdx.x] > sh[threadIdx.x + w] ? sh[threadIdx.x] : sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[f * gridDim.x + blockIdx.x] = sh[0];
+}
+
+static __global__ void absmax_final(const double *partial, int nblk, double *out) {
+  const int f = threadIdx.x;
+  if (f < NF) {
+    double a = 0;
+    for (int i = 0; i < nblk; ++i) a = partial[f * nblk + i] > a ? partial[f * nblk + i] : a;
+    out[f] = a;
+  }
 }
 
 static __global__ void sumsq_final(const double *partial, int nblk, double *out) {
@@ -280,6 +319,12 @@ struct Impl : Backend {
   int table_size(int het, int stress) const override {
     if (het) return stress ? GenSweep<R, 1>::NK_STRESS : GenSweep<R, 1>::NK_VELOCITY;
     return stress ? GenSweep<R, 0>::NK_STRESS : GenSweep<R, 0>::NK_VELOCITY;
+  }
+
+  void absmax(const DevState &s, int level, double *d_out9, cudaStream_t st) override {
+    const int nblk = 128;
+    absmax_partial<S><<<dim3(nblk, NF), 256, 0, st>>>(s, level, s.d_partial);
+    absmax_final<<<1, 32, 0, st>>>(s.d_partial, nblk, d_out9);
   }
 
   void sumsq(const DevState &s, int level, double *d_out9, cudaStream_t st) override {

@@ -555,6 +555,16 @@ int ofd_field_sumsq(ofd_handle *h, int level, double out[9]) {
   return OFD_OK;
 }
 
+int ofd_field_absmax(ofd_handle *h, int level, double out[9]) {
+  if (!h || !out) return fail(OFD_EINVAL, "null argument");
+  if (level < 0 || level > 1) return fail(OFD_EINVAL, "bad level %d", level);
+  h->be->absmax(h->s, level, h->d_out, h->stream);
+  OFD_CUDA(cudaGetLastError());
+  OFD_CUDA(cudaMemcpyAsync(out, h->d_out, sizeof(double) * NF, cudaMemcpyDeviceToHost, h->stream));
+  OFD_CUDA(cudaStreamSynchronize(h->stream));
+  return OFD_OK;
+}
+
 int ofd_field_view_get(ofd_handle *h, int field, int level, ofd_field_view *out) {
   int rc = check_fl(h, field, level);
   if (rc) return rc;

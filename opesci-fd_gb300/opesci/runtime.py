@@ -82,6 +82,7 @@ def load_library():
         'ofd_get_step': [h, P(ctypes.c_long)],
         'ofd_set_step': [h, ctypes.c_long],
         'ofd_field_sumsq': [h, ctypes.c_int, P(ctypes.c_double)],
+        'ofd_field_absmax': [h, ctypes.c_int, P(ctypes.c_double)],
         'ofd_field_view_get': [h, ctypes.c_int, ctypes.c_int, P(ofd_field_view)],
     }
     for name, args in sig.items():
@@ -264,6 +265,13 @@ class Simulation(object):
             level = self.steps % 2
         out = (ctypes.c_double * 9)()
         _check(self.lib.ofd_field_sumsq(self.h, level, out), 'ofd_field_sumsq')
+        return np.array(list(out))
+
+    def absmax(self, level=None):
+        if level is None:
+            level = self.steps % 2
+        out = (ctypes.c_double * 9)()
+        _check(self.lib.ofd_field_absmax(self.h, level, out), 'ofd_field_absmax')
         return np.array(list(out))
 
     @property
