@@ -111,12 +111,26 @@ int ofd_apply_boundary_init(ofd_handle *h, int level);
  * on the handle's stream. */
 int ofd_step(ofd_handle *h, int nsteps);
 int ofd_sync(ofd_handle *h);
+/* Non-blocking: 0 when all work queued on the handle has finished, 1 while
+ * some is still running, < 0 on error (serving loops poll with it). */
+int ofd_query(ofd_handle *h);
 /* ofd_step with CUDA events recorded on the handle's stream around every
  * kernel class of every step; waits for completion.  ms_total is the time
  * from the first to the last event; ms_class[k] the summed device time of
  * class k: 0 stress sweep, 1 stress ghosts, 2 velocity sweep, 3 velocity
  * ghosts and source.  launches (may be NULL) receives the kernel count. */
 int ofd_step_profiled(ofd_handle *h, int nsteps, double *ms_total, double ms_class[4], long *launches);
+/* ofd_step through a cached CUDA graph of two steps (one per starting
+ * parity), replayed nsteps/2 times; an odd remainder runs as a plain step.
+ * The source index is read on the device, so replays stay exact.  The graph
+ * is rebuilt after ofd_set_coefficients, ofd_set_source or ofd_set_tuning. */
+int ofd_step_graph(ofd_handle *h, int nsteps);
+/* Launch knobs chosen by the autotuner (opesci.autotune), no counterpart in
+ * the reference (which tuned Pluto tile sizes, tests/pluto_tile_test.py):
+ * per-sweep kernel (0 TMA-tiled, 1 plain), x-chunking multiplier (CTA waves,
+ * 1..64), plain-kernel block shape (bx multiple of 32, bx*by <= 256). */
+int ofd_set_tuning(ofd_handle *h, int stress_variant, int velocity_variant, int chunk_waves, int plain_bx,
+                   int plain_by);
 /* completed steps; the newest level is steps % 2 */
 int ofd_get_step(ofd_handle *h, long *steps);
 int ofd_set_step(ofd_handle *h, long steps);

@@ -29,6 +29,9 @@ struct DevState {
   double *d_partial;   // reduction scratch (>= 2048 doubles)
   long *d_step;        // device step counter (graph-safe source index)
   TiledCtx tiled;      // TMA descriptors for the tiled sweeps
+  // launch tuning (autotuner knobs): per-sweep variant 0 tiled / 1 plain,
+  // target waves for the x chunking, plain-kernel block shape
+  int var_stress, var_velocity, chunk_waves, plain_bx, plain_by;
   int het;             // 1: media arrays are factors of the update (read mode)
   int nks, nkv;        // literal-table sizes (0 until ofd_set_coefficients)
   float Ks[OFD_MAX_K], Kv[OFD_MAX_K];
@@ -50,6 +53,9 @@ struct Backend {
   virtual void from_padded(const DevState &s, float *dense, int f, int level, cudaStream_t st) = 0;
   virtual void sumsq(const DevState &s, int level, double *d_out9, cudaStream_t st) = 0;
   virtual void absmax(const DevState &s, int level, double *d_out9, cudaStream_t st) = 0;
+  // one-time launch attributes (dynamic shared memory) so that later launches
+  // can be captured into graphs
+  virtual void prepare(const DevState &s) = 0;
   // literal-table sizes of the generated expressions for media mode het
   virtual int table_size(int het, int stress) const = 0;
 };
@@ -247,7 +253,8 @@ struct Impl : Backend {
     SweepArgs<S> a = sweep_args(s, t0, stress);
     const Geom &g = s.g;
     const int nx = g.n1 - 2 * g.m, ny = g.n2 - 2 * g.m, nz = g.n3 - 2 * g.m;
-    if (s.variant != 1 && s.tiled.maps && tiled_supported<R, S>(g)) {
+    const int var = s.variant == 1 ? 1 : (stress ? s.var_stress : s.var_velocity);
+    if (var != 1 && s.tiled.maps && tiled_supported<R, S>(g)) {
       if (s.het) {
         if (stress) launch_stress_tiled<R, S, 1>(a, s.tiled, t0, st);
         else launch_velocity_tiled<R, S, 1>(a, s.tiled, t0, st);
@@ -257,11 +264,13 @@ struct Impl : Backend {
       }
       return;
     }
-    // plain: aim for >= 4 waves of 152 SMs
-    dim3 blk(32, 8);
-    dim3 grd((nz + 31) / 32, (ny + 7) / 8, 1);
+    // plain: aim for chunk_waves waves of 152 SMs x 8 CTAs
+    const int bx = s.plain_bx > 0 ? s.plain_bx : 32, by = s.plain_by > 0 ? s.plain_by : 8;
+    dim3 blk(bx, by);
+    dim3 grd((nz + bx - 1) / bx, (ny + by - 1) / by, 1);
     long ctas = (long)grd.x * grd.y;
-    int chunks = (int)((152L * 8 + ctas - 1) / ctas);
+    const int waves = s.chunk_waves > 0 ? s.chunk_waves : 1;
+    int chunks = (int)((152L * 8 * waves + ctas - 1) / ctas);
     if (chunks < 1) chunks = 1;
     if (chunks > nx) chunks = nx;
     a.xchunk = (nx + chunks - 1) / chunks;
@@ -314,6 +323,14 @@ struct Impl : Backend {
 
   void from_padded(const DevState &s, float *dense, int f, int level, cudaStream_t st) override {
     padded_to_dense<S><<<1216, 256, 0, st>>>(fp(s, f, level), dense, s.g, 1.f / s.scale[f]);
+  }
+
+  void prepare(const DevState &s) override {
+    if (s.het) {
+      prepare_tiled<R, S, 1>();
+    } else {
+      prepare_tiled<R, S, 0>();
+    }
   }
 
   int table_size(int het, int stress) const override {

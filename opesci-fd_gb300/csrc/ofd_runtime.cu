@@ -97,7 +97,16 @@ struct ofd_handle {
   double *d_out = nullptr;      // 16 doubles
   int *d_err = nullptr;         // error word of bounded device waits
   TmaMaps *maps = nullptr;      // TMA descriptors (host copy)
+  cudaGraphExec_t graph2[2] = {nullptr, nullptr};   // two-step graphs by starting parity
 };
+
+static void drop_graphs(ofd_handle *h) {
+  for (int p = 0; p < 2; ++p)
+    if (h->graph2[p]) {
+      cudaGraphExecDestroy(h->graph2[p]);
+      h->graph2[p] = nullptr;
+    }
+}
 
 namespace {
 
@@ -296,6 +305,11 @@ int ofd_create(const ofd_config *cfg, ofd_handle **out) {
   for (int i = 0; i < 3; ++i) h->s.h[i] = cfg->spacing[i];
   for (int k = 0; k < 4; ++k) h->s.c[k] = cfg->weights[k];
   h->s.variant = cfg->kernel_variant;
+  h->s.var_stress = 0;
+  h->s.var_velocity = 0;
+  h->s.chunk_waves = 1;
+  h->s.plain_bx = 32;
+  h->s.plain_by = 8;
   h->s.het = 0;
   h->s.nks = h->s.nkv = 0;
   switch (cfg->storage) {
@@ -307,6 +321,7 @@ int ofd_create(const ofd_config *cfg, ofd_handle **out) {
   h->s.tiled.maps = nullptr;
   h->s.tiled.err = h->d_err;
   h->s.tiled.z0 = L.z0;
+  h->s.tiled.waves = 1;
   if (build_maps(h)) h->s.tiled.maps = h->maps;
   e = cudaStreamSynchronize(h->stream);
   if (e != cudaSuccess || !h->be) {
@@ -321,6 +336,7 @@ int ofd_create(const ofd_config *cfg, ofd_handle **out) {
 int ofd_destroy(ofd_handle *h) {
   if (!h) return OFD_OK;
   if (h->stream) cudaStreamSynchronize(h->stream);
+  drop_graphs(h);
   delete h->be;
   delete h->maps;
   if (h->s.d_wav) cudaFree(h->s.d_wav);
@@ -345,6 +361,9 @@ int ofd_set_coefficients(ofd_handle *h, int het, const float *ks, int nks, const
   h->s.nkv = nkv;
   for (int i = 0; i < nks; ++i) h->s.Ks[i] = ks[i];
   for (int i = 0; i < nkv; ++i) h->s.Kv[i] = kv[i];
+  h->be->prepare(h->s);
+  drop_graphs(h);
+  OFD_CUDA(cudaGetLastError());
   return OFD_OK;
 }
 
@@ -459,6 +478,7 @@ int ofd_set_source(ofd_handle *h, int sx, int sy, int sz, const float *wavelet, 
   OFD_CUDA(cudaMemcpy(h->s.d_wav, wavelet, sizeof(float) * nt, cudaMemcpyHostToDevice));
   h->s.nt = nt;
   h->s.src_off = (long)sx * g.plane + (long)sy * g.P + sz;
+  drop_graphs(h);
   return OFD_OK;
 }
 
@@ -537,6 +557,62 @@ int ofd_step_profiled(ofd_handle *h, int nsteps, double *ms_total, double ms_cla
   for (int i = 0; i < nsteps; ++i)
     for (int k = 0; k < 8; ++k) cudaEventDestroy(evs[i].ev[k]);
   return check_err_word(h);
+}
+
+int ofd_set_tuning(ofd_handle *h, int stress_variant, int velocity_variant, int chunk_waves, int plain_bx,
+                   int plain_by) {
+  if (!h) return fail(OFD_EINVAL, "null handle");
+  if (stress_variant < 0 || stress_variant > 1 || velocity_variant < 0 || velocity_variant > 1)
+    return fail(OFD_EINVAL, "variants are 0 (tiled) or 1 (plain)");
+  if (chunk_waves < 1 || chunk_waves > 64) return fail(OFD_EINVAL, "chunk_waves must be in [1, 64]");
+  if (plain_bx < 1 || plain_by < 1 || plain_bx * plain_by > 256 || plain_bx % 32)
+    return fail(OFD_EINVAL, "plain block must be a multiple of 32 wide and at most 256 threads");
+  h->s.var_stress = stress_variant;
+  h->s.var_velocity = velocity_variant;
+  h->s.chunk_waves = chunk_waves;
+  h->s.tiled.waves = chunk_waves;
+  h->s.plain_bx = plain_bx;
+  h->s.plain_by = plain_by;
+  drop_graphs(h);
+  return OFD_OK;
+}
+
+int ofd_step_graph(ofd_handle *h, int nsteps) {
+  if (!h) return fail(OFD_EINVAL, "null handle");
+  if (nsteps < 0) return fail(OFD_EINVAL, "nsteps < 0");
+  if (h->s.nks == 0) return fail(OFD_ESTATE, "ofd_set_coefficients has not been called");
+  int done = 0;
+  while (nsteps - done >= 2) {
+    const int p = (int)(h->steps & 1);
+    if (!h->graph2[p]) {
+      cudaGraph_t g = nullptr;
+      OFD_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+      h->be->step(h->s, p, h->stream);
+      h->be->step(h->s, 1 - p, h->stream);
+      cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+      if (e != cudaSuccess) return fail(OFD_ECUDA, "graph capture failed: %s", cudaGetErrorString(e));
+      e = cudaGraphInstantiate(&h->graph2[p], g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return fail(OFD_ECUDA, "graph instantiation failed: %s", cudaGetErrorString(e));
+    }
+    OFD_CUDA(cudaGraphLaunch(h->graph2[p], h->stream));
+    h->steps += 2;
+    done += 2;
+  }
+  if (done < nsteps) {
+    h->be->step(h->s, (int)(h->steps & 1), h->stream);
+    h->steps += 1;
+  }
+  OFD_CUDA(cudaGetLastError());
+  return OFD_OK;
+}
+
+int ofd_query(ofd_handle *h) {
+  if (!h) return fail(OFD_EINVAL, "null handle");
+  const cudaError_t e = cudaStreamQuery(h->stream);
+  if (e == cudaSuccess) return 0;
+  if (e == cudaErrorNotReady) return 1;
+  return fail(OFD_ECUDA, "cudaStreamQuery: %s", cudaGetErrorString(e));
 }
 
 int ofd_sync(ofd_handle *h) {

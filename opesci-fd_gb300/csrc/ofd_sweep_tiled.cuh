@@ -44,6 +44,7 @@ struct TiledCtx {
   const TmaMaps *maps;   // nullptr: descriptors unavailable, use plain kernels
   int *err;              // device error word
   int z0;                // element offset of z = 0 in a padded row
+  int waves;             // CTA-count multiplier (autotuner knob), 1 = default
 };
 
 // Box extents the runtime encodes into the descriptors.
@@ -85,11 +86,22 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
   return ok != 0;
 }
 
-// Bounded wait; false when the limit ran out.
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Bounded wait; false when 10 s of wall time ran out (a time bound, not an
+// iteration count, so heavy concurrent load never trips it spuriously).
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
-  for (long it = 0; it < (1L << 24); ++it)
-    if (mbar_try_wait(bar, parity)) return true;
-  return false;
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = global_ns();
+  for (;;) {
+    for (int i = 0; i < 64; ++i)
+      if (mbar_try_wait(bar, parity)) return true;
+    if (global_ns() - t0 > 10000000000ULL) return false;
+  }
 }
 
 __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, uint64_t *bar, int c0, int c1, int c2) {
@@ -358,17 +370,29 @@ void launch_tiled(const SweepArgs<S> &a, const TiledCtx &ctx, int t0, cudaStream
   p.ntz = (nz + TZ - 1) / TZ;
   p.nty = (ny + G::TY - 1) / G::TY;
   const long tiles = (long)p.ntz * p.nty;
-  // enough CTAs for ~8 waves of 152 SMs at the resident count, chunks >= 16 planes
+  // enough CTAs for ~8 waves (x ctx.waves) of 152 SMs at the resident count,
+  // chunks >= 16 planes
   const int per_sm = (227 * 1024) / (G::SMEM + 1024) > 0 ? (227 * 1024) / (G::SMEM + 1024) : 1;
-  long want = 152L * per_sm * 8;
+  long want = 152L * per_sm * 8 * (ctx.waves > 0 ? ctx.waves : 1);
   int chunks = (int)((want + tiles - 1) / tiles);
   if (chunks > nx / 16) chunks = nx / 16;
   if (chunks < 1) chunks = 1;
   p.chunk = (nx + chunks - 1) / chunks;
   chunks = (nx + p.chunk - 1) / p.chunk;
   auto kern = sweep_tiled<R, S, HET, STRESS>;
-  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM);
   kern<<<dim3((unsigned)tiles, (unsigned)chunks), G::THREADS, G::SMEM, st>>>(a, p);
+}
+
+// Dynamic shared memory opt-in of both sweeps; called once per handle so that
+// launches can later be captured in a CUDA graph.
+template <int R, typename S, int HET>
+void prepare_tiled() {
+  if (tiled_fits<R, S, HET, true>())
+    cudaFuncSetAttribute(sweep_tiled<R, S, HET, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         TiledCfg<R, S, HET, true>::SMEM);
+  if (tiled_fits<R, S, HET, false>())
+    cudaFuncSetAttribute(sweep_tiled<R, S, HET, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         TiledCfg<R, S, HET, false>::SMEM);
 }
 
 template <int R, typename S, int HET>

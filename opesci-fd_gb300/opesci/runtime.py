@@ -77,8 +77,11 @@ def load_library():
         'ofd_set_source': [h, ctypes.c_int, ctypes.c_int, ctypes.c_int, fptr, ctypes.c_int],
         'ofd_apply_boundary_init': [h, ctypes.c_int],
         'ofd_step': [h, ctypes.c_int],
+        'ofd_step_graph': [h, ctypes.c_int],
+        'ofd_set_tuning': [h, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int],
         'ofd_step_profiled': [h, ctypes.c_int, P(ctypes.c_double), P(ctypes.c_double), P(ctypes.c_long)],
         'ofd_sync': [h],
+        'ofd_query': [h],
         'ofd_get_step': [h, P(ctypes.c_long)],
         'ofd_set_step': [h, ctypes.c_long],
         'ofd_field_sumsq': [h, ctypes.c_int, P(ctypes.c_double)],
@@ -236,6 +239,14 @@ class Simulation(object):
     def step(self, n=1):
         _check(self.lib.ofd_step(self.h, int(n)), 'ofd_step')
 
+    def step_graph(self, n):
+        """Advance n steps by replaying a captured two-step CUDA graph."""
+        _check(self.lib.ofd_step_graph(self.h, int(n)), 'ofd_step_graph')
+
+    def set_tuning(self, stress_variant=0, velocity_variant=0, chunk_waves=1, plain_bx=32, plain_by=8):
+        _check(self.lib.ofd_set_tuning(self.h, int(stress_variant), int(velocity_variant), int(chunk_waves),
+                                       int(plain_bx), int(plain_by)), 'ofd_set_tuning')
+
     def step_profiled(self, n):
         """Advance n steps with CUDA events on the handle's stream; returns
         (total ms, [stress sweep, stress ghosts, velocity sweep, velocity
@@ -246,6 +257,13 @@ class Simulation(object):
         _check(self.lib.ofd_step_profiled(self.h, int(n), ctypes.byref(tot), cls, ctypes.byref(nl)),
                'ofd_step_profiled')
         return tot.value, list(cls), nl.value
+
+    def done(self):
+        """True when all work queued on this simulation has finished."""
+        rc = self.lib.ofd_query(self.h)
+        if rc < 0:
+            _check(rc, 'ofd_query')
+        return rc == 0
 
     def sync(self):
         _check(self.lib.ofd_sync(self.h), 'ofd_sync')

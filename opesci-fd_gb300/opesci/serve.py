@@ -1,0 +1,208 @@
+"""Serving forward-modelling requests with continuous batching on one GPU.
+
+Requests (grid edge log-uniform in [48, 384], space order 4 or 8, 200-2000
+steps, FP32 or scaled-FP16 storage, seeded layered media and Ricker source)
+arrive as a Poisson stream.  The server admits a waiting request as soon as
+its device footprint fits the HBM budget (150 GB by default), keeps its nine
+fields and media resident, and advances every admitted request in slices of
+``slice_steps`` time steps (captured CUDA graphs on the request's own stream).
+Requests that arrive while others run join at the next slice boundary, their
+work overlaps on the device, and a finished request frees its memory for the
+queue.  The baseline serves the same stream one request at a time with
+per-kernel launches.
+
+    python -m opesci.serve --requests 40 --rates 0.5 1 2
+
+prints a JSON object: per rate, p50/p99 latency and aggregate GLUP/s for both
+servers, and the largest difference between a request's result served in the
+mix and served alone (FP64 sums of squares of its nine final fields).
+"""
+import argparse
+import json
+import math
+import os
+import time
+from collections import deque
+
+import numpy as np
+
+from . import runtime, autotune
+from .batch import Shot, _weights
+
+# Fixed FP16 storage scales for these layered problems (unit Ricker source):
+# velocities ~1e-7 m/s, stresses ~1 Pa, from the precision study's magnitudes
+# with 16x headroom.
+FP16_SCALES = [2.0 ** 30] * 3 + [2.0 ** 9] * 3 + [2.0 ** 10] * 3
+
+
+class Request(object):
+    def __init__(self, rid, arrival, shot, storage):
+        self.id, self.arrival, self.shot, self.storage = rid, arrival, shot, storage
+        self.admitted = self.finished = None
+
+    @property
+    def lups(self):
+        return self.shot.lups
+
+
+def make_requests(count, rate, seed=0, edge_range=(48, 384), so_choices=(4, 8), steps_range=(200, 2000),
+                  fp16_fraction=0.25, f_range=(8.0, 25.0)):
+    """Seeded requests; the jobs depend on ``seed`` only and the Poisson
+    arrival times (mean gap 1/rate) on a second stream, so a rate sweep
+    serves the same jobs at different loads."""
+    rng = np.random.default_rng(seed)
+    arr = np.random.default_rng(seed + 1)
+    t = 0.0
+    out = []
+    for i in range(count):
+        t += arr.exponential(1.0) / rate
+        n = int(round(math.exp(rng.uniform(math.log(edge_range[0]), math.log(edge_range[1])))))
+        so = int(rng.choice(so_choices))
+        steps = int(rng.integers(steps_range[0], steps_range[1] + 1))
+        f0 = float(rng.uniform(*f_range))
+        storage = 'f16' if rng.uniform() < fp16_fraction else 'f32'
+        out.append(Request(i, t, Shot(n, so, steps, seed * 7777 + i, f0), storage))
+    return out
+
+
+def footprint(req):
+    m = req.shot.so // 2
+    dims = (req.shot.n + 2 * m,) * 3
+    cfg = runtime.make_config(dims, req.shot.so, [10.0] * 3, 1e-3, _weights(req.shot.so), storage=req.storage)
+    return runtime.Simulation.footprint(cfg)
+
+
+def open_request(req, built, tuned=True):
+    cfg, media, src, wav, ks, kv = built
+    scales = FP16_SCALES if req.storage == 'f16' else None
+    c = runtime.make_config(list(cfg.dim), cfg.space_order, list(cfg.spacing), cfg.dt, list(cfg.weights),
+                            storage=req.storage, free_surface=list(cfg.free_surface), field_scale=scales)
+    sim = runtime.Simulation(c)
+    sim.set_coefficients(1, ks, kv)
+    sim.set_media(*media)
+    sim.set_source(src, wav)
+    if tuned and req.storage == 'f32':
+        sim.set_tuning(**autotune.tune(c, ks, kv, het=1))
+    return sim
+
+
+def _finish_stats(reqs, t_first, t_last):
+    lat = np.array([r.finished - r.arrival for r in reqs])
+    lups = sum(r.lups for r in reqs)
+    return {'p50_s': float(np.percentile(lat, 50)), 'p99_s': float(np.percentile(lat, 99)),
+            'mean_s': float(lat.mean()), 'glups': lups / (t_last - t_first) / 1e9,
+            'makespan_s': t_last - t_first}
+
+
+def serve_continuous(reqs, built, budget_bytes=150e9, slice_steps=32, max_active=96, checks=None):
+    """Continuous batching.  ``checks`` (dict) receives each request's FP64
+    sums of squares of its final fields."""
+    t0 = time.perf_counter()
+    pending = deque(sorted(reqs, key=lambda r: r.arrival))
+    queue = deque()
+    active = []          # [req, sim, remaining, bytes]
+    used = 0
+    while pending or queue or active:
+        now = time.perf_counter() - t0
+        while pending and pending[0].arrival <= now:
+            queue.append(pending.popleft())
+        while queue and len(active) < max_active:
+            r = queue[0]
+            fp = footprint(r)
+            if active and used + fp > budget_bytes:
+                break
+            queue.popleft()
+            r.admitted = time.perf_counter() - t0
+            active.append([r, open_request(r, built[r.id]), r.shot.steps, fp])
+            used += fp
+        if not active:
+            if pending:
+                time.sleep(max(0.0, pending[0].arrival - (time.perf_counter() - t0)))
+            continue
+        progressed = False
+        for a in list(active):
+            r, sim, rem, fp = a
+            if sim.done():
+                if rem == 0:
+                    sim.sync()          # raises if any device wait of the request expired
+                    r.finished = time.perf_counter() - t0
+                    if checks is not None:
+                        checks[r.id] = sim.sumsq().tolist()
+                    sim.close()
+                    used -= fp
+                    active.remove(a)
+                else:
+                    # keep two slices in flight per request
+                    k = min(2 * slice_steps, rem)
+                    sim.step_graph(k)
+                    a[2] = rem - k
+                progressed = True
+        if not progressed:
+            time.sleep(50e-6)
+    t_first = min(r.arrival for r in reqs)
+    t_last = max(r.finished for r in reqs)
+    return _finish_stats(reqs, t_first, t_last)
+
+
+def serve_one_by_one(reqs, built, checks=None):
+    """Baseline: one request at a time in arrival order, per-kernel launches."""
+    t0 = time.perf_counter()
+    for r in sorted(reqs, key=lambda r: r.arrival):
+        now = time.perf_counter() - t0
+        if r.arrival > now:
+            time.sleep(r.arrival - now)
+        r.admitted = time.perf_counter() - t0
+        sim = open_request(r, built[r.id], tuned=False)
+        sim.step(r.shot.steps)
+        sim.sync()
+        r.finished = time.perf_counter() - t0
+        if checks is not None:
+            checks[r.id] = sim.sumsq().tolist()
+        sim.close()
+    t_first = min(r.arrival for r in reqs)
+    t_last = max(r.finished for r in reqs)
+    return _finish_stats(reqs, t_first, t_last)
+
+
+def max_rel_diff(a, b):
+    worst = 0.0
+    for k in a:
+        x, y = np.array(a[k]), np.array(b[k])
+        d = np.abs(x - y) / np.maximum(np.abs(y), 1e-300)
+        worst = max(worst, float(d.max()))
+    return worst
+
+
+def main():
+    ap = argparse.ArgumentParser(description='continuous-batching server vs one request at a time')
+    ap.add_argument('--requests', type=int, default=40)
+    ap.add_argument('--rates', type=float, nargs='+', default=[0.5, 1.0, 2.0])
+    ap.add_argument('--seed', type=int, default=0)
+    ap.add_argument('--budget-gb', type=float, default=150.0)
+    ap.add_argument('--max-edge', type=int, default=384)
+    args = ap.parse_args()
+    os.environ.setdefault('CUDA_DEVICE_MAX_CONNECTIONS', '32')
+    out = {'requests': args.requests, 'rates': {}}
+    jobs = make_requests(args.requests, 1.0, seed=args.seed, edge_range=(48, args.max_edge))
+    built = {r.id: r.shot.build() for r in jobs}
+    for r in jobs:
+        if r.storage == 'f32':
+            b = built[r.id]
+            autotune.tune(b[0], b[4], b[5], het=1)
+    out['jobs'] = [dict(r.shot.to_dict(), storage=r.storage) for r in jobs]
+    for rate in args.rates:
+        reqs = make_requests(args.requests, rate, seed=args.seed, edge_range=(48, args.max_edge))
+        chk_c, chk_p = {}, {}
+        cont = serve_continuous(reqs, built, budget_bytes=args.budget_gb * 1e9, checks=chk_c)
+        plain = serve_one_by_one(reqs, built, checks=chk_p)
+        out['rates'][str(rate)] = {
+            'continuous': cont, 'one_by_one': plain,
+            'glups_ratio': cont['glups'] / plain['glups'],
+            'max_rel_diff_alone_vs_mix': max_rel_diff(chk_c, chk_p),
+            'fp16_requests': sum(1 for r in reqs if r.storage == 'f16'),
+            'glup': sum(r.lups for r in reqs) / 1e9}
+    print(json.dumps(out))
+
+
+if __name__ == '__main__':
+    main()

@@ -106,6 +106,26 @@ def sweep_tables(grid):
     return out
 
 
+def _unit_grid(space_order):
+    """Heterogeneous model with dt = 1 and unit spacing: its literals are the
+    exact rationals r_i of the update expressions (K_i = r_i dt / h)."""
+    from ..models import elastic_grid
+    return elastic_grid((13.0, 13.0, 13.0), (13, 13, 13), 1.0, 10.0, space_order=space_order,
+                        read=True, rho_file='r', vp_file='p', vs_file='s', analytic=False,
+                        free_surface=False)
+
+
+def het_tables(space_order, dt, h):
+    """Literal tables of the heterogeneous update expressions for isotropic
+    spacing h and time step dt, from the stored unit tables: every literal of
+    these expressions is a rational times dt/h.  Returns float32 (ks, kv)."""
+    sig = prebuilt_signatures()['so%d_het' % space_order]
+    f = float(dt) / float(h)
+    ks = np.array([np.float32(float(r) * f) for r in sig['unit_stress']], dtype=np.float32)
+    kv = np.array([np.float32(float(r) * f) for r in sig['unit_velocity']], dtype=np.float32)
+    return ks, kv
+
+
 def _variant_grid(space_order, hetero):
     from ..models import elastic_grid
     if hetero:
@@ -135,6 +155,15 @@ def generate_headers(outdir):
             key = 'so%d_%s' % (so, 'het' if het else 'const')
             sigs[key] = {'stress': signature(se), 'velocity': signature(ve),
                          'nk_stress': len(sl), 'nk_velocity': len(vl)}
+            if het:
+                ug = _unit_grid(so)
+                uby = {f.label.name: f for f in ug.fields}
+                use, usl = kernel_text(ug, [uby[n] for n in STRESS_ORDER])
+                uve, uvl = kernel_text(ug, [uby[n] for n in VELOCITY_ORDER])
+                if signature(use) != sigs[key]['stress'] or signature(uve) != sigs[key]['velocity']:
+                    raise RuntimeError('unit-step structure differs for %s' % key)
+                sigs[key]['unit_stress'] = usl
+                sigs[key]['unit_velocity'] = uvl
             lines.append('template <> struct GenSweep<%d, %d> {' % (so // 2, het))
             lines.append('  static constexpr bool ok = true;')
             lines.append('  static constexpr int NK_STRESS = %d, NK_VELOCITY = %d;' % (len(sl), len(vl)))
