@@ -475,7 +475,10 @@ int ofd_set_source(ofd_handle *h, int sx, int sy, int sz, const float *wavelet, 
     h->s.d_wav = nullptr;
   }
   OFD_CUDA(cudaMalloc((void **)&h->s.d_wav, sizeof(float) * nt));
-  OFD_CUDA(cudaMemcpy(h->s.d_wav, wavelet, sizeof(float) * nt, cudaMemcpyHostToDevice));
+  // stream-ordered copy: a plain cudaMemcpy from pageable memory may return
+  // before its DMA lands and is not ordered with this non-blocking stream
+  OFD_CUDA(cudaMemcpyAsync(h->s.d_wav, wavelet, sizeof(float) * nt, cudaMemcpyHostToDevice, h->stream));
+  OFD_CUDA(cudaStreamSynchronize(h->stream));
   h->s.nt = nt;
   h->s.src_off = (long)sx * g.plane + (long)sy * g.P + sz;
   drop_graphs(h);
@@ -522,8 +525,8 @@ static int check_err_word(ofd_handle *h) {
   OFD_CUDA(cudaMemcpyAsync(&err, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
   OFD_CUDA(cudaStreamSynchronize(h->stream));
   if (err) {
-    int zero = 0;
-    cudaMemcpy(h->d_err, &zero, sizeof(int), cudaMemcpyHostToDevice);
+    cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream);
+    cudaStreamSynchronize(h->stream);
     return fail(OFD_ETIMEOUT, "a bounded device wait expired in a tiled sweep (error word %d)", err);
   }
   return OFD_OK;

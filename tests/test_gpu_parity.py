@@ -169,3 +169,32 @@ def test_error_paths_leave_context_usable():
     sim.sync()
     assert np.isfinite(sim.sumsq()).all()
     sim.close()
+
+
+def test_source_upload_is_ordered_while_gpu_busy():
+    """A handle's inputs must be ordered with its own stream even while other
+    handles keep the GPU busy (an unordered wavelet upload once let the first
+    source injections read a partly copied wavelet under load)."""
+    busy_g, busy_media, busy_src, busy_wav = layered_problem(160, space_order=4, ntsteps=400, seed=7)
+    busy = runtime.Simulation(runtime.config_from_grid(busy_g))
+    busy.set_coefficients_from_grid(busy_g)
+    busy.set_media(*busy_media)
+    busy.set_source(busy_src, busy_wav)
+    g, media, src, wav = layered_problem(40, space_order=4, ntsteps=60, seed=8)
+    alone = run_problem_gpu(g, media, src, wav)
+    results = []
+    for _ in range(3):
+        busy.step(150)                      # keeps the device busy meanwhile
+        sim = runtime.Simulation(runtime.config_from_grid(g))
+        sim.set_coefficients_from_grid(g)
+        sim.set_media(*media)
+        sim.set_source(src, wav)
+        sim.step_graph(60)
+        sim.sync()
+        results.append({f: sim.download(f) for f in runtime.FIELDS})
+        sim.close()
+    busy.sync()
+    busy.close()
+    for r in results:
+        for f in runtime.FIELDS:
+            assert np.array_equal(r[f], alone[f]), f
