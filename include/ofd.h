@@ -131,6 +131,12 @@ int ofd_step_graph(ofd_handle *h, int nsteps);
  * 1..64), plain-kernel block shape (bx multiple of 32, bx*by <= 256). */
 int ofd_set_tuning(ofd_handle *h, int stress_variant, int velocity_variant, int chunk_waves, int plain_bx,
                    int plain_by);
+/* Persistent time stepping (no counterpart in the reference): when enabled,
+ * ofd_step and ofd_step_graph run up to 1024 whole steps per cooperative
+ * launch, with grid barriers between the phases of a step.  For small grids,
+ * whose steps are shorter than the launches they would otherwise need.
+ * Results are identical to the per-kernel path. */
+int ofd_set_persistent(ofd_handle *h, int enable);
 /* completed steps; the newest level is steps % 2 */
 int ofd_get_step(ofd_handle *h, long *steps);
 int ofd_set_step(ofd_handle *h, long steps);

@@ -35,6 +35,15 @@
 
 namespace ofd {
 
+// Global loads of field values: COH = true reads through L2 only
+// (ld.global.cg), which a kernel needs when it reads values that other CTAs
+// wrote earlier in the same launch (the persistent step kernel).
+template <bool COH, typename S>
+__device__ __forceinline__ S ldg(const S *p) {
+  if (COH) return __ldcg(p);
+  return *p;
+}
+
 __device__ __forceinline__ void plane_axes(int d, int &a1, int &a2) {
   // a2 is the faster-varying in-plane axis (mapped to threadIdx.x)
   if (d == 0) { a1 = 1; a2 = 2; }
@@ -58,17 +67,14 @@ __device__ __forceinline__ int mu_pair(int a, int b) {
   return M_MU23;
 }
 
-// Stress ghosts of face normal a.d: blockIdx.z = field(0..5)*2 + side.
-template <int R, typename S>
-__global__ void __launch_bounds__(256) stress_bc_kernel(BcArgs<S> a) {
+// Stress ghosts of face normal d at in-plane point (i1, i2) for stress
+// component fi (0..5) and side.
+template <int R, typename S, bool COH>
+__device__ __forceinline__ void stress_bc_point(const BcArgs<S> &a, int d, int i1, int i2, int fi, int side) {
   typedef typename Storage<S>::C C;
-  const Geom g = a.g;
-  const int d = a.d;
+  const Geom &g = a.g;
   int a1, a2;
   plane_axes(d, a1, a2);
-  const int i2 = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i1 = blockIdx.y * blockDim.y + threadIdx.y;
-  const int fi = blockIdx.z >> 1, side = blockIdx.z & 1;
   const int n1 = gdim(g, a1), n2 = gdim(g, a2), nd = gdim(g, d);
   if (i1 >= n1 || i2 >= n2) return;
   const int fb = a.face[2 * d + side];
@@ -91,7 +97,7 @@ __global__ void __launch_bounds__(256) stress_bc_kernel(BcArgs<S> a) {
       const int sgn = side == 0 ? -1 : 1;
 #pragma unroll
       for (int k = 1; k < R; ++k) {
-        const C v = Storage<S>::load(T[base + (b - sgn * k) * sd], a.inv[F]);
+        const C v = Storage<S>::load(ldg<COH>(&T[base + (b - sgn * k) * sd]), a.inv[F]);
         T[base + (b + sgn * k) * sd] = Storage<S>::store(-v, a.sc[F]);
       }
     } else {
@@ -99,7 +105,7 @@ __global__ void __launch_bounds__(256) stress_bc_kernel(BcArgs<S> a) {
       for (int k = 0; k < R; ++k) {
         const int dst = side == 0 ? b - 1 - k : b + k;
         const int src = side == 0 ? b + k : b - 1 - k;
-        const C v = Storage<S>::load(T[base + src * sd], a.inv[F]);
+        const C v = Storage<S>::load(ldg<COH>(&T[base + src * sd]), a.inv[F]);
         T[base + dst * sd] = Storage<S>::store(-v, a.sc[F]);
       }
     }
@@ -117,29 +123,34 @@ __global__ void __launch_bounds__(256) stress_bc_kernel(BcArgs<S> a) {
   const C K1 = l2m - q, K2 = lam - q;
   const long sa = gstride(g, ax), se = gstride(g, e);
   const S *va = a.f0[F_U + ax], *ve = a.f0[F_U + e];
-  auto LV = [&](const S *p, int f, long off) -> C { return Storage<S>::load(p[o + off], a.inv[f]); };
+  auto LV = [&](const S *p, int f, long off) -> C { return Storage<S>::load(ldg<COH>(&p[o + off]), a.inv[f]); };
   const C Da = (a.c4[0] * (LV(va, F_U + ax, 0) - LV(va, F_U + ax, -sa)) +
                 a.c4[1] * (LV(va, F_U + ax, sa) - LV(va, F_U + ax, -2 * sa))) / a.h[ax];
   const C De = (a.c4[0] * (LV(ve, F_U + e, 0) - LV(ve, F_U + e, -se)) +
                 a.c4[1] * (LV(ve, F_U + e, se) - LV(ve, F_U + e, -2 * se))) / a.h[e];
-  const C t0 = Storage<S>::load(a.f0[F][o], a.inv[F]);
+  const C t0 = Storage<S>::load(ldg<COH>(&a.f0[F][o]), a.inv[F]);
   T[o] = Storage<S>::store(t0 + a.dt * (K1 * Da + K2 * De), a.sc[F]);
 }
 
-// Velocity ghosts of face normal a.d.  sub 0: blockIdx.z = side (component
-// along d); sub 1: blockIdx.z = which tangential component (0/1)*2 + side.
+// Stress ghosts of face normal a.d: blockIdx.z = field(0..5)*2 + side.
 template <int R, typename S>
-__global__ void __launch_bounds__(256) velocity_bc_kernel(BcArgs<S> a) {
-  typedef typename Storage<S>::C C;
-  const Geom g = a.g;
-  const int d = a.d;
-  int a1, a2;
-  plane_axes(d, a1, a2);
+__global__ void __launch_bounds__(256) stress_bc_kernel(BcArgs<S> a) {
   const int i2 = blockIdx.x * blockDim.x + threadIdx.x;
   const int i1 = blockIdx.y * blockDim.y + threadIdx.y;
+  stress_bc_point<R, S, false>(a, a.d, i1, i2, blockIdx.z >> 1, blockIdx.z & 1);
+}
+
+// Velocity ghosts of face normal d at in-plane point (i1, i2).  sub 0: the
+// component along d, zi = side; sub 1: zi = which tangential component * 2 + side.
+template <int R, typename S, bool COH>
+__device__ __forceinline__ void velocity_bc_point(const BcArgs<S> &a, int d, int sub, int i1, int i2, int zi) {
+  typedef typename Storage<S>::C C;
+  const Geom &g = a.g;
+  int a1, a2;
+  plane_axes(d, a1, a2);
   const int n1 = gdim(g, a1), n2 = gdim(g, a2), nd = gdim(g, d);
   if (i1 < 1 || i1 >= n1 - 1 || i2 < 1 || i2 >= n2 - 1) return;
-  const int side = blockIdx.z & 1;
+  const int side = zi & 1;
   const int fb = a.face[2 * d + side];
   if (fb == 0) return;
   const int m = g.m;
@@ -148,7 +159,7 @@ __global__ void __launch_bounds__(256) velocity_bc_kernel(BcArgs<S> a) {
   c[a1] = i1; c[a2] = i2; c[d] = 0;
   const long base = lin(g, c[0], c[1], c[2]);
   const long sd = gstride(g, d);
-  const int comp = (a.sub == 0) ? d : ((blockIdx.z >> 1) == 0 ? a1 : a2);
+  const int comp = (sub == 0) ? d : ((zi >> 1) == 0 ? a1 : a2);
   const int F = F_U + comp;
   S *v = a.f1[F];
   if (fb == 2) {  // Robertsson
@@ -162,7 +173,7 @@ __global__ void __launch_bounds__(256) velocity_bc_kernel(BcArgs<S> a) {
     }
     return;
   }
-  auto LD = [&](int f, long off) -> C { return Storage<S>::load(a.f1[f][off], a.inv[f]); };
+  auto LD = [&](int f, long off) -> C { return Storage<S>::load(ldg<COH>(&a.f1[f][off]), a.inv[f]); };
   if (comp == d) {
     const long ob = base + b * sd;
     const C lam = (C)a.media[M_LAM][ob], mu = (C)a.media[M_MU][ob];
@@ -197,6 +208,15 @@ __global__ void __launch_bounds__(256) velocity_bc_kernel(BcArgs<S> a) {
     const C val = LD(F, ob) - G0 + (mu_lo / mu_hi) * (LD(F, ob) - LD(F, obm) + Gm);
     v[ob + sd] = Storage<S>::store(val, a.sc[F]);
   }
+}
+
+// Velocity ghosts of face normal a.d.  sub 0: blockIdx.z = side (component
+// along d); sub 1: blockIdx.z = which tangential component (0/1)*2 + side.
+template <int R, typename S>
+__global__ void __launch_bounds__(256) velocity_bc_kernel(BcArgs<S> a) {
+  const int i2 = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i1 = blockIdx.y * blockDim.y + threadIdx.y;
+  velocity_bc_point<R, S, false>(a, a.d, a.sub, i1, i2, blockIdx.z);
 }
 
 template <typename S>

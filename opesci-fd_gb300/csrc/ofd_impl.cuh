@@ -7,6 +7,7 @@
 #include "ofd_sweep_plain.cuh"
 #include "ofd_sweep_tiled.cuh"
 #include "ofd_bc.cuh"
+#include "ofd_persistent.cuh"
 
 namespace ofd {
 
@@ -32,6 +33,8 @@ struct DevState {
   // launch tuning (autotuner knobs): per-sweep variant 0 tiled / 1 plain,
   // target waves for the x chunking, plain-kernel block shape
   int var_stress, var_velocity, chunk_waves, plain_bx, plain_by;
+  int persistent;      // 1: time steps run in one cooperative launch
+  unsigned *d_bar;     // grid-barrier words of the persistent kernel
   int het;             // 1: media arrays are factors of the update (read mode)
   int nks, nkv;        // literal-table sizes (0 until ofd_set_coefficients)
   float Ks[OFD_MAX_K], Kv[OFD_MAX_K];
@@ -56,6 +59,9 @@ struct Backend {
   // one-time launch attributes (dynamic shared memory) so that later launches
   // can be captured into graphs
   virtual void prepare(const DevState &s) = 0;
+  // nsteps whole steps in one cooperative launch starting at parity p0;
+  // returns a cudaError_t
+  virtual int step_persistent(const DevState &s, int p0, int nsteps, cudaStream_t st) = 0;
   // literal-table sizes of the generated expressions for media mode het
   virtual int table_size(int het, int stress) const = 0;
 };
@@ -331,6 +337,43 @@ struct Impl : Backend {
     } else {
       prepare_tiled<R, S, 0>();
     }
+  }
+
+  int step_persistent(const DevState &s, int p0, int nsteps, cudaStream_t st) override {
+    PersistArgs<S> a;
+    for (int p = 0; p < 2; ++p) {
+      a.st[p] = sweep_args(s, p, true);
+      a.ve[p] = sweep_args(s, p, false);
+      a.sbc[p] = bc_args(s, 1 - p, p, s.legacy ? 0 : 1);
+      a.vbc[p] = bc_args(s, 1 - p, 1 - p, 0);
+    }
+    a.src_off = s.src_off;
+    a.wav = s.d_wav;
+    a.nt = s.nt;
+    a.d_step = s.d_step;
+    a.ssc[0] = s.scale[F_TXX];
+    a.ssc[1] = s.scale[F_TYY];
+    a.ssc[2] = s.scale[F_TZZ];
+    a.bar = s.d_bar;
+    a.err = s.tiled.err;
+    a.nsteps = nsteps;
+    a.p0 = p0;
+    void *kern = s.het ? (void *)persistent_steps_kernel<R, S, 1> : (void *)persistent_steps_kernel<R, S, 0>;
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, 0);
+    const Geom &g = s.g;
+    const long npts = (long)(g.n1 - 2 * g.m) * (g.n2 - 2 * g.m) * (g.n3 - 2 * g.m);
+    long want = (npts + 1023) / 1024;
+    if (want < 16) want = 16;
+    const long cap = (long)sms * (per_sm > 0 ? per_sm : 1);
+    const unsigned blocks = (unsigned)(want < cap ? want : cap);
+    void *args[] = {&a};
+    // barrier words start from zero for every launch (an expired barrier of
+    // an earlier launch may have left arrivals behind)
+    cudaMemsetAsync(s.d_bar, 0, 2 * sizeof(unsigned), st);
+    return (int)cudaLaunchCooperativeKernel(kern, dim3(blocks), dim3(256), args, 0, st);
   }
 
   int table_size(int het, int stress) const override {

@@ -293,6 +293,8 @@ int ofd_create(const ofd_config *cfg, ofd_handle **out) {
   h->s.d_step = (long *)(extra + 2 * 4096 + 1024);
   h->d_out = (double *)(extra + 2 * 4096 + 2048);
   h->d_err = (int *)(extra + 3 * 4096);
+  h->s.d_bar = (unsigned *)(extra + 3 * 4096 + 256);
+  h->s.persistent = 0;
   h->s.d_wav = nullptr;
   h->s.src_off = -1;
   h->s.nt = 0;
@@ -507,10 +509,35 @@ int ofd_get_step(ofd_handle *h, long *steps) {
   return OFD_OK;
 }
 
+// nsteps in cooperative launches of at most 1024 steps each
+static int run_persistent(ofd_handle *h, int nsteps) {
+  int done = 0;
+  while (done < nsteps) {
+    const int k = nsteps - done < 1024 ? nsteps - done : 1024;
+    const int e = h->be->step_persistent(h->s, (int)(h->steps & 1), k, h->stream);
+    if (e != (int)cudaSuccess)
+      return fail(OFD_ECUDA, "persistent launch failed: %s", cudaGetErrorString((cudaError_t)e));
+    h->steps += k;
+    done += k;
+  }
+  return OFD_OK;
+}
+
+int ofd_set_persistent(ofd_handle *h, int enable) {
+  if (!h) return fail(OFD_EINVAL, "null handle");
+  int dev = 0, coop = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+  if (enable && !coop) return fail(OFD_EINVAL, "device has no cooperative launch");
+  h->s.persistent = enable ? 1 : 0;
+  return OFD_OK;
+}
+
 int ofd_step(ofd_handle *h, int nsteps) {
   if (!h) return fail(OFD_EINVAL, "null handle");
   if (nsteps < 0) return fail(OFD_EINVAL, "nsteps < 0");
   if (h->s.nks == 0) return fail(OFD_ESTATE, "ofd_set_coefficients has not been called");
+  if (h->s.persistent) return run_persistent(h, nsteps);
   for (int i = 0; i < nsteps; ++i) {
     const int t0 = (int)(h->steps & 1);
     h->be->step(h->s, t0, h->stream);
@@ -584,6 +611,7 @@ int ofd_step_graph(ofd_handle *h, int nsteps) {
   if (!h) return fail(OFD_EINVAL, "null handle");
   if (nsteps < 0) return fail(OFD_EINVAL, "nsteps < 0");
   if (h->s.nks == 0) return fail(OFD_ESTATE, "ofd_set_coefficients has not been called");
+  if (h->s.persistent) return run_persistent(h, nsteps);
   int done = 0;
   while (nsteps - done >= 2) {
     const int p = (int)(h->steps & 1);

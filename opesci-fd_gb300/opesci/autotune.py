@@ -1,8 +1,9 @@
 """Autotuner of the device runtime's launch knobs (the reference searched Pluto
 tile sizes with a pybench sweep, tests/pluto_tile_test.py:9-54).
 
-Knobs (ofd_set_tuning): per-sweep kernel (0 TMA-tiled, 1 plain), the x
-chunking multiplier (CTA waves) and the plain kernel's block shape.  Each
+Knobs (ofd_set_tuning, ofd_set_persistent): per-sweep kernel (0 TMA-tiled,
+1 plain), the x chunking multiplier (CTA waves), the plain kernel's block
+shape, and persistent stepping (whole steps in one cooperative launch).  Each
 candidate runs a few profiled steps on a scratch handle of the same shape
 (zero fields, constant media: the kernels' cost does not depend on values),
 the fastest is kept, and results are cached in a JSON file keyed by grid
@@ -16,7 +17,8 @@ import threading
 from . import runtime
 
 _lock = threading.Lock()
-DEFAULT = {'stress_variant': 0, 'velocity_variant': 0, 'chunk_waves': 1, 'plain_bx': 32, 'plain_by': 8}
+DEFAULT = {'stress_variant': 0, 'velocity_variant': 0, 'chunk_waves': 1, 'plain_bx': 32, 'plain_by': 8,
+           'persistent': 0}
 
 
 def cache_path():
@@ -48,14 +50,22 @@ def _save(d):
 
 
 def _time(sim, knobs, steps):
+    """ms per step of graph (or persistent) stepping, best of two runs."""
+    import time
     sim.set_tuning(**knobs)
-    sim.step(2)
+    sim.step_graph(2)
     sim.sync()
-    ms, cls, _ = sim.step_profiled(steps)
-    return ms / steps
+    best = None
+    for _ in range(2):
+        t0 = time.perf_counter()
+        sim.step_graph(steps)
+        sim.sync()
+        t = (time.perf_counter() - t0) * 1e3 / steps
+        best = t if best is None else min(best, t)
+    return best
 
 
-def tune(cfg, ks, kv, het=1, steps=6, use_cache=True):
+def tune(cfg, ks, kv, het=1, steps=20, use_cache=True):
     """Best knobs for configuration ``cfg`` with literal tables ks/kv."""
     key = _key(cfg, het)
     with _lock:
@@ -89,6 +99,12 @@ def tune(cfg, ks, kv, het=1, steps=6, use_cache=True):
                 results.append((k, t))
                 if t < best_t:
                     best, best_t = k, t
+        # persistent stepping: all phases of many steps in one launch
+        k = dict(best, persistent=1)
+        t = _time(sim, k, steps)
+        results.append((k, t))
+        if t < best_t:
+            best, best_t = k, t
     finally:
         sim.close()
     if use_cache:

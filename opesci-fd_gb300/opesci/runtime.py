@@ -78,6 +78,7 @@ def load_library():
         'ofd_apply_boundary_init': [h, ctypes.c_int],
         'ofd_step': [h, ctypes.c_int],
         'ofd_step_graph': [h, ctypes.c_int],
+        'ofd_set_persistent': [h, ctypes.c_int],
         'ofd_set_tuning': [h, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int],
         'ofd_step_profiled': [h, ctypes.c_int, P(ctypes.c_double), P(ctypes.c_double), P(ctypes.c_long)],
         'ofd_sync': [h],
@@ -243,9 +244,15 @@ class Simulation(object):
         """Advance n steps by replaying a captured two-step CUDA graph."""
         _check(self.lib.ofd_step_graph(self.h, int(n)), 'ofd_step_graph')
 
-    def set_tuning(self, stress_variant=0, velocity_variant=0, chunk_waves=1, plain_bx=32, plain_by=8):
+    def set_persistent(self, enable=True):
+        """Run time steps in cooperative launches of up to 1024 steps."""
+        _check(self.lib.ofd_set_persistent(self.h, 1 if enable else 0), 'ofd_set_persistent')
+
+    def set_tuning(self, stress_variant=0, velocity_variant=0, chunk_waves=1, plain_bx=32, plain_by=8,
+                   persistent=0):
         _check(self.lib.ofd_set_tuning(self.h, int(stress_variant), int(velocity_variant), int(chunk_waves),
                                        int(plain_bx), int(plain_by)), 'ofd_set_tuning')
+        self.set_persistent(bool(persistent))
 
     def step_profiled(self, n):
         """Advance n steps with CUDA events on the handle's stream; returns

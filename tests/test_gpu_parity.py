@@ -198,3 +198,27 @@ def test_source_upload_is_ordered_while_gpu_busy():
     for r in results:
         for f in runtime.FIELDS:
             assert np.array_equal(r[f], alone[f]), f
+
+
+@pytest.mark.parametrize('so,n,storage', [(4, 40, 'f32'), (8, 36, 'f32'), (4, 33, 'f16'), (6, 30, 'f32')])
+def test_persistent_steps_identical(so, n, storage):
+    """Whole steps in one cooperative launch (grid barriers between phases)
+    give the per-kernel results bit for bit, across launch chunks and odd
+    step counts."""
+    g, media, src, wav = layered_problem(n, space_order=so, ntsteps=37, seed=13)
+    scales = [2.0 ** 30] * 3 + [2.0 ** 9] * 6 if storage == 'f16' else None
+    out = []
+    for persistent in (False, True):
+        sim = runtime.Simulation(runtime.config_from_grid(g, storage=storage, field_scale=scales))
+        sim.set_coefficients_from_grid(g)
+        sim.set_media(*media)
+        sim.set_source(src, wav)
+        sim.set_persistent(persistent)
+        sim.step(11)
+        sim.step_graph(26)
+        sim.sync()
+        out.append({f: sim.download(f) for f in runtime.FIELDS})
+        sim.close()
+    for f in runtime.FIELDS:
+        assert np.array_equal(out[0][f], out[1][f]), f
+    assert np.abs(out[1]['Txx']).max() > 0
