@@ -8,6 +8,7 @@
 #include <vector>
 
 #include <cuda.h>
+#include <mutex>
 
 #include "ofd.h"
 #include "ofd_impl.cuh"
@@ -185,8 +186,31 @@ CUtensorMapDataType tma_type(int storage) {
   return CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
 }
 
+// cuTensorMapEncodeTiled, looked up through the runtime's driver entry
+// point so that the library does not link libcuda itself and loads on
+// machines without a driver (it fails at ofd_create there instead).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+  });
+  return fn;
+}
+
 // 3D descriptor over one level: dims (P, n2, n1), rows of P elements.
 bool encode(CUtensorMap *m, void *level_base, CUtensorMapDataType t, size_t es, const Geom &g, int bw, int bh) {
+  EncodeTiledFn cuTensorMapEncodeTiled = encode_fn();
+  if (!cuTensorMapEncodeTiled) return false;
   cuuint64_t dims[3] = {(cuuint64_t)g.P, (cuuint64_t)g.n2, (cuuint64_t)g.n1};
   cuuint64_t strides[2] = {(cuuint64_t)(g.P * es), (cuuint64_t)(g.plane * es)};
   cuuint32_t box[3] = {(cuuint32_t)bw, (cuuint32_t)bh, 1};
@@ -324,6 +348,10 @@ int ofd_create(const ofd_config *cfg, ofd_handle **out) {
   h->s.tiled.err = h->d_err;
   h->s.tiled.z0 = L.z0;
   h->s.tiled.waves = 1;
+  if (!encode_fn()) {
+    ofd_destroy(h);
+    return fail(OFD_ECUDA, "the driver does not provide cuTensorMapEncodeTiled");
+  }
   if (build_maps(h)) h->s.tiled.maps = h->maps;
   e = cudaStreamSynchronize(h->stream);
   if (e != cudaSuccess || !h->be) {

@@ -67,7 +67,7 @@ def build(force=False, verbose=False, extra_flags=()):
     with ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(compile_one, srcs))
     tmp = LIBNAME + '.tmp'
-    cmd = [cc] + ARCH + ['-shared', '-o', tmp] + objs + ['-lcuda']
+    cmd = [cc] + ARCH + ['-shared', '-o', tmp] + objs
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError('nvcc link failed:\n%s\n%s' % (' '.join(cmd), r.stderr[-4000:]))
