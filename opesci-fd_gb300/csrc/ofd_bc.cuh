@@ -6,9 +6,11 @@
 // normal (x, then y, then z), and later faces read values written by earlier
 // ones (corners, and the Levander recompute overwriting planes a mirror has
 // read).  One launch per face normal d reproduces that: within a phase the
-// fields and the two sides are independent.  Velocity ghosts need two
-// launches per normal: the component along d first (staggeredgrid.py:829-832),
-// then the two tangential components that read it.
+// fields and the two sides are independent.  Velocity ghosts of one normal
+// are ordered too: the component along d first (staggeredgrid.py:829-832),
+// then the two tangential components that read it at their point and at the
+// next point along their own axis; the kernel below recomputes that
+// neighbour's value instead of reading it, so one launch per normal suffices.
 //
 // Stress, face normal d, plane index b (lower b = m, upper b = n-m-1):
 //  * normal stress T_dd (unstaggered along d): T[b] = 0, T[b-+k] = -T[b+-k],
@@ -210,31 +212,121 @@ __device__ __forceinline__ void velocity_bc_point(const BcArgs<S> &a, int d, int
   }
 }
 
-// Velocity ghosts of face normal a.d.  sub 0: blockIdx.z = side (component
-// along d); sub 1: blockIdx.z = which tangential component (0/1)*2 + side.
-template <int R, typename S>
-__global__ void __launch_bounds__(256) velocity_bc_kernel(BcArgs<S> a) {
-  const int i2 = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i1 = blockIdx.y * blockDim.y + threadIdx.y;
-  velocity_bc_point<R, S, false>(a, a.d, a.sub, i1, i2, blockIdx.z);
+// Levander ghost value of the component along d at in-plane point (i1, i2)
+// of side `side` (the value velocity_bc_point writes for sub 0).
+template <typename S, bool COH>
+__device__ __forceinline__ typename Storage<S>::C levander_normal_ghost(const BcArgs<S> &a, int d, int side,
+                                                                        int i1, int i2) {
+  typedef typename Storage<S>::C C;
+  const Geom &g = a.g;
+  int a1, a2;
+  plane_axes(d, a1, a2);
+  const int nd = gdim(g, d);
+  const int b = side == 0 ? g.m : nd - g.m - 1;
+  int c[3];
+  c[a1] = i1; c[a2] = i2; c[d] = 0;
+  const long sd = gstride(g, d);
+  const long ob = lin(g, c[0], c[1], c[2]) + b * sd;
+  const int F = F_U + d;
+  auto LD = [&](int f, long off) -> C { return Storage<S>::load(ldg<COH>(&a.f1[f][off]), a.inv[f]); };
+  const C lam = (C)a.media[M_LAM][ob], mu = (C)a.media[M_MU][ob];
+  const C r = lam / (lam + C(2) * mu);
+  C s = 0;
+#pragma unroll
+  for (int t = 0; t < 2; ++t) {
+    const int j = t == 0 ? a1 : a2;
+    const long sj = gstride(g, j);
+    s += (a.h[d] / a.h[j]) * (LD(F_U + j, ob) - LD(F_U + j, ob - sj));
+  }
+  return side == 0 ? LD(F, ob) + r * s : LD(F, ob - sd) - r * s;
 }
 
-template <typename S>
-__global__ void source_kernel(S *txx, S *tyy, S *tzz, long off, const float *w, int nt,
-                              const long *step, float s0, float s1, float s2) {
-  const long st = *step;
-  if (st < nt) {
-    const float v = w[st] / 3;
-    txx[off] = Storage<S>::store(Storage<S>::load(txx[off], 1.f / s0) - v, s0);
-    tyy[off] = Storage<S>::store(Storage<S>::load(tyy[off], 1.f / s1) - v, s1);
-    tzz[off] = Storage<S>::store(Storage<S>::load(tzz[off], 1.f / s2) - v, s2);
+// All velocity ghosts of face normal d at in-plane point (i1, i2): the
+// component along d, then the two tangential components, which need the new
+// along-d ghost at this point and at the next point along their own axis.
+// That neighbour value is recomputed here from the same inputs (where the
+// neighbour lies inside the along-d range) instead of read after another
+// thread wrote it, so one launch per face normal gives the two-phase result.
+template <int R, typename S, bool COH>
+__device__ __forceinline__ void velocity_bc_merged_point(const BcArgs<S> &a, int d, int i1, int i2) {
+  typedef typename Storage<S>::C C;
+  const Geom &g = a.g;
+  int a1, a2;
+  plane_axes(d, a1, a2);
+  const int n1 = gdim(g, a1), n2 = gdim(g, a2), nd = gdim(g, d);
+  if (i1 < 1 || i1 >= n1 - 1 || i2 < 1 || i2 >= n2 - 1) return;
+  const long sd = gstride(g, d);
+  const int Fd = F_U + d;
+  for (int side = 0; side < 2; ++side) {
+    const int fb = a.face[2 * d + side];
+    if (fb == 0) continue;
+    if (fb == 2) {
+      velocity_bc_point<R, S, COH>(a, d, 0, i1, i2, side);
+      velocity_bc_point<R, S, COH>(a, d, 1, i1, i2, side);
+      velocity_bc_point<R, S, COH>(a, d, 1, i1, i2, 2 + side);
+      continue;
+    }
+    const int b = side == 0 ? g.m : nd - g.m - 1;
+    int c[3];
+    c[a1] = i1; c[a2] = i2; c[d] = 0;
+    const long base = lin(g, c[0], c[1], c[2]);
+    const long ob = base + b * sd, obm = ob - sd;
+    const long gpos = side == 0 ? obm : ob;        // where the along-d ghost lives
+    const C vg = levander_normal_ghost<S, COH>(a, d, side, i1, i2);
+    a.f1[Fd][gpos] = Storage<S>::store(vg, a.sc[Fd]);
+    auto LD = [&](int f, long off) -> C { return Storage<S>::load(ldg<COH>(&a.f1[f][off]), a.inv[f]); };
+    for (int t = 0; t < 2; ++t) {
+      const int j = t == 0 ? a1 : a2;
+      const long sj = gstride(g, j);
+      // along-d ghost at the next point along j: recomputed when the
+      // two-phase order would have written it first, else the stored value
+      const int n1j = t == 0 ? i1 + 1 : i1, n2j = t == 0 ? i2 : i2 + 1;
+      const bool in = n1j >= 1 && n1j < n1 - 1 && n2j >= 1 && n2j < n2 - 1;
+      const C vgn = in ? Storage<S>::load(Storage<S>::store(levander_normal_ghost<S, COH>(a, d, side, n1j, n2j),
+                                                            a.sc[Fd]), a.inv[Fd])
+                       : LD(Fd, gpos + sj);
+      const C vg0 = Storage<S>::load(Storage<S>::store(vg, a.sc[Fd]), a.inv[Fd]);
+      const int F = F_U + j;
+      const int mp = mu_pair(j, d);
+      const C mu_lo = (C)a.media[mp][obm], mu_hi = (C)a.media[mp][ob];
+      const C hr = a.h[d] / a.h[j];
+      if (side == 0) {
+        const C Gm = hr * (vgn - vg0);                          // G(b-1), ghost plane
+        const C G0 = hr * (LD(Fd, ob + sj) - LD(Fd, ob));        // G(b)
+        const C val = LD(F, ob) + Gm - (mu_hi / mu_lo) * (LD(F, ob + sd) - LD(F, ob) + G0);
+        a.f1[F][obm] = Storage<S>::store(val, a.sc[F]);
+      } else {
+        const C Gm = hr * (LD(Fd, obm + sj) - LD(Fd, obm));      // G(b-1)
+        const C G0 = hr * (vgn - vg0);                          // G(b), ghost plane
+        const C val = LD(F, ob) - G0 + (mu_lo / mu_hi) * (LD(F, ob) - LD(F, obm) + Gm);
+        a.f1[F][ob + sd] = Storage<S>::store(val, a.sc[F]);
+      }
+    }
   }
 }
 
-}  // namespace ofd
+// One launch per face normal; the first (d = 0) also applies the point
+// source to the new stresses and advances the device step counter (step !=
+// nullptr), which commutes with the velocity ghosts (disjoint arrays).  A
+// captured step graph replays with unchanged arguments: the wavelet sample is
+// picked on the device from the step counter.
+template <int R, typename S>
+__global__ void __launch_bounds__(256) velocity_bc_merged_kernel(BcArgs<S> a, S *txx, S *tyy, S *tzz, long src_off,
+                                                                 const float *w, int nt, long *step, float s0,
+                                                                 float s1, float s2) {
+  const int i2 = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i1 = blockIdx.y * blockDim.y + threadIdx.y;
+  velocity_bc_merged_point<R, S, false>(a, a.d, i1, i2);
+  if (step != nullptr && a.d == 0 && i1 == 0 && i2 == 0) {
+    const long st = *step;
+    if (src_off >= 0 && st < nt) {
+      const float v = w[st] / 3;
+      txx[src_off] = Storage<S>::store(Storage<S>::load(txx[src_off], 1.f / s0) - v, s0);
+      tyy[src_off] = Storage<S>::store(Storage<S>::load(tyy[src_off], 1.f / s1) - v, s1);
+      tzz[src_off] = Storage<S>::store(Storage<S>::load(tzz[src_off], 1.f / s2) - v, s2);
+    }
+    *step = st + 1;
+  }
+}
 
-namespace ofd {
-// Advances the device-side step counter read by source_kernel, so that a
-// captured step graph can be replayed without host-side arguments changing.
-static __global__ void step_tick(long *step) { *step += 1; }
 }  // namespace ofd

@@ -244,14 +244,16 @@ struct Impl : Backend {
     }
   }
 
-  void velocity_bc(const DevState &s, int t1, cudaStream_t st) {
+  // Velocity ghosts, one launch per face normal.  with_source: the first
+  // launch also applies the source to the level-t1 stresses and advances the
+  // device step counter (time stepping); boundary_init passes false.
+  void velocity_bc(const DevState &s, int t1, bool with_source, cudaStream_t st) {
     BcArgs<S> a = bc_args(s, t1, t1, 0);
     for (int d = 0; d < 3; ++d) {
       a.d = d;
-      a.sub = 0;
-      velocity_bc_kernel<R, S><<<face_grid(s.g, d, 2), dim3(32, 8), 0, st>>>(a);
-      a.sub = 1;
-      velocity_bc_kernel<R, S><<<face_grid(s.g, d, 4), dim3(32, 8), 0, st>>>(a);
+      velocity_bc_merged_kernel<R, S><<<face_grid(s.g, d, 1), dim3(32, 8), 0, st>>>(
+          a, fp(s, F_TXX, t1), fp(s, F_TYY, t1), fp(s, F_TZZ, t1), with_source ? s.src_off : -1L, s.d_wav, s.nt,
+          with_source ? s.d_step : nullptr, s.scale[F_TXX], s.scale[F_TYY], s.scale[F_TZZ]);
     }
   }
 
@@ -303,24 +305,19 @@ struct Impl : Backend {
     sweeps(s, t0, false, st);
     rec(5);
     rec(6);
-    velocity_bc(s, t1, st);
-    if (s.src_off >= 0) {
-      source_kernel<S><<<1, 1, 0, st>>>(fp(s, F_TXX, t1), fp(s, F_TYY, t1), fp(s, F_TZZ, t1), s.src_off,
-                                        s.d_wav, s.nt, s.d_step, s.scale[F_TXX], s.scale[F_TYY],
-                                        s.scale[F_TZZ]);
-    }
-    step_tick<<<1, 1, 0, st>>>(s.d_step);
+    velocity_bc(s, t1, true, st);
     rec(7);
   }
 
   int launches_per_step(const DevState &s) const override {
-    // 2 sweeps + 3 stress-ghost phases + 6 velocity-ghost phases + source + tick
-    return 2 + 3 + 6 + (s.src_off >= 0 ? 1 : 0) + 1;
+    // 2 sweeps + 3 stress-ghost phases + 3 velocity-ghost phases (the first
+    // carries the source and the step counter)
+    return 2 + 3 + 3;
   }
 
   void boundary_init(const DevState &s, int level, cudaStream_t st) override {
     stress_bc(s, level, level, 0, st);
-    velocity_bc(s, level, st);
+    velocity_bc(s, level, false, st);
   }
 
   void to_padded(const DevState &s, const float *dense, int f, int level, cudaStream_t st) override {

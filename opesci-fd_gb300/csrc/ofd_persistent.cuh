@@ -1,8 +1,8 @@
 // Persistent time stepping for small grids: one cooperative launch advances
 // a simulation many steps.  Every phase of a step (stress sweep, three stress
-// ghost phases, velocity sweep, six velocity ghost phases with the source)
+// ghost phases, velocity sweep, three velocity ghost phases with the source)
 // is a grid-stride loop over the whole grid, separated by a grid barrier, so
-// a step costs 11 barriers instead of 13 kernel launches.  Small grids, whose
+// a step costs 8 barriers instead of 8 kernel launches.  Small grids, whose
 // steps are shorter than a few kernel launches, are the ones that gain.
 //
 // The barrier is this library's own: a counter and a generation word in
@@ -145,36 +145,30 @@ __global__ void __launch_bounds__(256) persistent_steps_kernel(const __grid_cons
       }
     }
     if (!grid_barrier(a.bar, a.err)) return;
-    // velocity ghosts: per face normal the component along it, then the
-    // other two; the source and the step counter ride on the first phase
+    // velocity ghosts, one phase per face normal; the source and the step
+    // counter ride on the first
     for (int d = 0; d < 3; ++d) {
       int a1, a2;
       plane_axes(d, a1, a2);
       const int n1 = gdim(g, a1), n2 = gdim(g, a2);
-      for (int sub = 0; sub < 2; ++sub) {
-        const int nz2 = sub == 0 ? 2 : 4;
-        const long nitems = (long)n1 * n2 * nz2;
-        for (long i = gtid; i < nitems; i += gstride) {
-          const int i2 = (int)(i % n2);
-          const long r = i / n2;
-          const int i1 = (int)(r % n1);
-          velocity_bc_point<R, S, true>(a.vbc[p], d, sub, i1, i2, (int)(r / n1));
-        }
-        if (d == 0 && sub == 0 && gtid == 0) {
-          const long st = *(volatile long *)a.d_step;
-          if (a.src_off >= 0 && st < a.nt) {
-            const float v = a.wav[st] / 3;
-            S *t[3] = {a.st[p].out[F_TXX], a.st[p].out[F_TYY], a.st[p].out[F_TZZ]};
-#pragma unroll
-            for (int q = 0; q < 3; ++q) {
-              const C old = Storage<S>::load(__ldcg(&t[q][a.src_off]), 1.f / a.ssc[q]);
-              t[q][a.src_off] = Storage<S>::store(old - v, a.ssc[q]);
-            }
-          }
-          *a.d_step = st + 1;
-        }
-        if (!grid_barrier(a.bar, a.err)) return;
+      const long nitems = (long)n1 * n2;
+      for (long i = gtid; i < nitems; i += gstride) {
+        velocity_bc_merged_point<R, S, true>(a.vbc[p], d, (int)(i / n2), (int)(i % n2));
       }
+      if (d == 0 && gtid == 0) {
+        const long st = *(volatile long *)a.d_step;
+        if (a.src_off >= 0 && st < a.nt) {
+          const float v = a.wav[st] / 3;
+          S *t[3] = {a.st[p].out[F_TXX], a.st[p].out[F_TYY], a.st[p].out[F_TZZ]};
+#pragma unroll
+          for (int q = 0; q < 3; ++q) {
+            const C old = Storage<S>::load(__ldcg(&t[q][a.src_off]), 1.f / a.ssc[q]);
+            t[q][a.src_off] = Storage<S>::store(old - v, a.ssc[q]);
+          }
+        }
+        *a.d_step = st + 1;
+      }
+      if (!grid_barrier(a.bar, a.err)) return;
     }
   }
 }
