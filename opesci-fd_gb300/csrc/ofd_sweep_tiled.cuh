@@ -7,11 +7,16 @@
 // (TZ + 2 ZH) x (TY + 2R) elements; a ring of NSH such planes holds the x
 // window [x-R, x+R] plus the planes in flight.  Arrays read only at the point
 // (the field being updated at t0, the media) arrive as TZ x TY boxes in a
-// second ring of NSC planes.  Each ring slot has an mbarrier; one thread
-// issues cp.async.bulk.tensor loads with complete_tx accounting, everyone
-// else waits on the slot's phase (bounded: a wait that runs out sets the
-// error word and the CTA drains its loads and returns).  Results go straight
-// to HBM with coalesced 128-byte row stores.
+// second ring of NSC planes.  The CTA is warp-specialised: one producer warp
+// (lane 0) issues the cp.async.bulk.tensor loads, each slot with a "full"
+// mbarrier (complete_tx accounting) and an "empty" mbarrier that the eight
+// consumer warps (one per tile row) arrive on when they are done with the
+// plane; the producer refills a slot once it is empty.  Consumers therefore
+// wait only for their data, never for each other (no CTA-wide barrier per
+// plane).  Every wait is bounded: one that runs out sets the error word and
+// the CTA's abort flag, the other warps leave their loops, and the producer
+// drains the loads in flight before the CTA exits.  Results go straight to
+// HBM with coalesced 128-byte row stores.
 //
 // The arithmetic is the generated expression (GenSweep) read through an
 // accessor that maps A(f, dx, dy, dz) onto the rings, so the tiled kernels
@@ -104,6 +109,23 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
   }
 }
 
+// Bounded wait that also returns false once another warp of the CTA has
+// aborted (*abort != 0).
+__device__ __forceinline__ bool mbar_wait_or_abort(uint64_t *bar, unsigned parity, volatile int *abort) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = global_ns();
+  for (;;) {
+    for (int i = 0; i < 64; ++i)
+      if (mbar_try_wait(bar, parity)) return true;
+    if (*abort) return false;
+    if (global_ns() - t0 > 10000000000ULL) return false;
+  }
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
 __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, uint64_t *bar, int c0, int c1, int c2) {
   asm volatile(
       "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], [%2];"
@@ -123,7 +145,8 @@ __host__ __device__ constexpr int round128(int b) { return (b + 127) / 128 * 128
 template <int R, typename S, int HET, bool STRESS>
 struct TiledCfg {
   static constexpr int TY = tile_rows(R);
-  static constexpr int THREADS = 32 * TY;
+  static constexpr int NCW = TY;                           // consumer warps (one per row)
+  static constexpr int THREADS = 32 * (TY + 1);            // + one producer warp
   static constexpr int ZH = ZHalo<S>::v;                  // z halo, rounded to 16 B
   static constexpr int HW = TZ + 2 * ZH;                   // halo box width
   static constexpr int HH = TY + 2 * R;                    // halo box height
@@ -146,7 +169,7 @@ struct TiledCfg {
   static constexpr int CSTAGE = NH0 * HSLOT + NPF * PSLOT + NMF * MSLOT;
   static constexpr int XRING = NSH * XSTAGE;
   static constexpr int CRING = NSC * CSTAGE;
-  static constexpr int BARS = (NSH + NSC) * 8;
+  static constexpr int BARS = 2 * (NSH + NSC) * 8;        // full and empty barrier per slot
   static constexpr int SMEM = XRING + CRING + round128(BARS) + 128;  // +128: base alignment
   static constexpr unsigned XBYTES = NXF * HBOX;
   static constexpr unsigned CBYTES = NH0 * HBOX + NPF * PBOX + NMF * MBOX;
@@ -198,7 +221,7 @@ struct TiledAcc {
   }
 };
 
-template <int R> struct TiledThreads { static constexpr int v = 32 * tile_rows(R); };
+template <int R> struct TiledThreads { static constexpr int v = 32 * (tile_rows(R) + 1); };
 
 template <int R, typename S, int HET, bool STRESS>
 __global__ void __launch_bounds__(TiledThreads<R>::v)
@@ -209,8 +232,10 @@ sweep_tiled(const __grid_constant__ SweepArgs<S> a, const __grid_constant__ Tile
   unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127);
   unsigned char *xring = smem;
   unsigned char *cring = smem + G::XRING;
-  uint64_t *xbar = (uint64_t *)(smem + G::XRING + G::CRING);
-  uint64_t *cbar = xbar + G::NSH;
+  uint64_t *xbar = (uint64_t *)(smem + G::XRING + G::CRING);   // x-window slots filled
+  uint64_t *cbar = xbar + G::NSH;                                // plane-ring slots filled
+  uint64_t *xemp = cbar + G::NSC;                                // x-window slots released
+  uint64_t *cemp = xemp + G::NSH;                                // plane-ring slots released
   __shared__ int abort_flag;
 
   const Geom &g = a.g;
@@ -246,85 +271,117 @@ sweep_tiled(const __grid_constant__ SweepArgs<S> a, const __grid_constant__ Tile
     for (int i = 0; i < G::NMF; ++i) tma_load_3d(st + G::moff(i), &p.mmap[i], bar, zc, y0, plane);
   };
 
-  int hissued = hq0 - 1, pissued = xb - 1;   // last plane issued (thread 0)
+  // Warp specialisation: warps 0..NCW-1 compute one row each; warp NCW is
+  // the producer, whose lane 0 issues every TMA load.  A slot is refilled
+  // once all consumer warps have released it (empty barrier, NCW arrivals),
+  // so consumers never wait on each other, only on their data.
+  const int warp = tid >> 5, lane = tid & 31;
   if (tid == 0) {
     abort_flag = 0;
-    for (int i = 0; i < G::NSH; ++i) mbar_init(&xbar[i], 1);
-    for (int i = 0; i < G::NSC; ++i) mbar_init(&cbar[i], 1);
+    for (int i = 0; i < G::NSH; ++i) { mbar_init(&xbar[i], 1); mbar_init(&xemp[i], G::NCW); }
+    for (int i = 0; i < G::NSC; ++i) { mbar_init(&cbar[i], 1); mbar_init(&cemp[i], G::NCW); }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    for (int pl = hq0; pl <= hlast && pl < hq0 + G::NSH; ++pl) { issue_x(pl); hissued = pl; }
-    for (int pl = xb; pl < xe && pl < xb + G::NSC; ++pl) { issue_c(pl); pissued = pl; }
   }
   __syncthreads();
 
-  const int yl = tid >> 5, lane = tid & 31;
-  const int y = y0 + yl;
-  int hwaited = hq0 - 1;   // last x-window plane waited for
-  int pwaited = xb - 1;    // last plane-ring plane waited for
-  bool ok = true;
-  for (int x = xb; x < xe && ok; ++x) {
-    for (int pl = hwaited + 1; pl <= x + R && ok; ++pl) {
-      const int q = pl - hq0;
-      if (!mbar_wait(&xbar[q % G::NSH], (unsigned)((q / G::NSH) & 1))) ok = false;
-      else hwaited = pl;
-    }
-    if (ok) {
-      const int q = x - xb;
-      if (!mbar_wait(&cbar[q % G::NSC], (unsigned)((q / G::NSC) & 1))) ok = false;
-      else pwaited = x;
-    }
-    if (!ok) {
-      atomicExch(p.err, 1);
-      abort_flag = 1;
-    }
-    __syncthreads();
-    if (abort_flag) break;
-    TiledAcc<R, S, HET, STRESS> A;
-#pragma unroll
-    for (int k = 0; k < 2 * R + 1; ++k) A.xs[k] = xring + ((x + k - R - hq0) % G::NSH) * G::XSTAGE;
-    A.cs = cring + ((x - xb) % G::NSC) * G::CSTAGE;
-    A.inv = a.inv;
-#pragma unroll
-    for (int half = 0; half < 2; ++half) {
-      const int zl = lane + 32 * half;
-      const int z = z0 + zl;
-      A.hpos = (yl + R) * G::HW + zl + G::ZH;
-      A.ppos = yl * TZ + zl;
-      const long o = (long)x * g.plane + (long)y * g.P + z;
-      const bool inside = (z < g.n3 - g.m) && (y < g.n2 - g.m);
-      if (STRESS) {
-        C out[6];
-        GenSweep<R, HET>::template stress<C>(A, a.K, out);
-        if (inside) {
-#pragma unroll
-          for (int i = 0; i < 6; ++i) a.out[F_TXX + i][o] = Storage<S>::store(out[i], a.sc[F_TXX + i]);
-        }
-      } else {
-        C out[3];
-        GenSweep<R, HET>::template velocity<C>(A, a.K, out);
-        if (inside) {
-#pragma unroll
-          for (int i = 0; i < 3; ++i) a.out[F_U + i][o] = Storage<S>::store(out[i], a.sc[F_U + i]);
+  int hissued = hq0 - 1, pissued = xb - 1;   // last plane issued (producer)
+  if (warp == G::NCW) {
+    if (lane == 0) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      for (int pl = hq0; pl <= hlast && pl < hq0 + G::NSH; ++pl) { issue_x(pl); hissued = pl; }
+      for (int pl = xb; pl < xe && pl < xb + G::NSC; ++pl) { issue_c(pl); pissued = pl; }
+      // then in the order the consumers need them: x-window plane P at
+      // iteration P - R, plane-ring plane P at iteration P
+      while (hissued < hlast || pissued < xe - 1) {
+        const bool take_x = hissued < hlast && (pissued >= xe - 1 || hissued + 1 - R <= pissued + 1);
+        if (take_x) {
+          const int q = hissued + 1 - hq0;
+          if (!mbar_wait_or_abort(&xemp[q % G::NSH], (unsigned)((q / G::NSH - 1) & 1), &abort_flag)) break;
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          issue_x(hissued + 1);
+          ++hissued;
+        } else {
+          const int q = pissued + 1 - xb;
+          if (!mbar_wait_or_abort(&cemp[q % G::NSC], (unsigned)((q / G::NSC - 1) & 1), &abort_flag)) break;
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          issue_c(pissued + 1);
+          ++pissued;
         }
       }
+      if (hissued < hlast || pissued < xe - 1) {
+        atomicExch(p.err, 1);
+        abort_flag = 1;
+      }
     }
-    __syncthreads();   // stages of plane x - R (x-window) and x (plane ring) are free
-    if (tid == 0) {
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      const int nh = x - R + G::NSH;
-      if (nh <= hlast) { issue_x(nh); hissued = nh; }
-      const int np = x + G::NSC;
-      if (np < xe) { issue_c(np); pissued = np; }
+  } else {
+    const int yl = warp;
+    const int y = y0 + yl;
+    int hwaited = hq0 - 1;   // last x-window plane waited for
+    for (int x = xb; x < xe; ++x) {
+      bool ok = true;
+      for (int pl = hwaited + 1; pl <= x + R && ok; ++pl) {
+        const int q = pl - hq0;
+        if (!mbar_wait_or_abort(&xbar[q % G::NSH], (unsigned)((q / G::NSH) & 1), &abort_flag)) ok = false;
+        else hwaited = pl;
+      }
+      if (ok) {
+        const int q = x - xb;
+        if (!mbar_wait_or_abort(&cbar[q % G::NSC], (unsigned)((q / G::NSC) & 1), &abort_flag)) ok = false;
+      }
+      // leave as a whole warp (the release below is warp-synchronous)
+      if (!__all_sync(0xffffffffu, ok)) {
+        if (lane == 0) {
+          atomicExch(p.err, 1);
+          abort_flag = 1;
+        }
+        break;
+      }
+      TiledAcc<R, S, HET, STRESS> A;
+#pragma unroll
+      for (int k = 0; k < 2 * R + 1; ++k) A.xs[k] = xring + ((x + k - R - hq0) % G::NSH) * G::XSTAGE;
+      A.cs = cring + ((x - xb) % G::NSC) * G::CSTAGE;
+      A.inv = a.inv;
+#pragma unroll
+      for (int half = 0; half < 2; ++half) {
+        const int zl = lane + 32 * half;
+        const int z = z0 + zl;
+        A.hpos = (yl + R) * G::HW + zl + G::ZH;
+        A.ppos = yl * TZ + zl;
+        const long o = (long)x * g.plane + (long)y * g.P + z;
+        const bool inside = (z < g.n3 - g.m) && (y < g.n2 - g.m);
+        if (STRESS) {
+          C out[6];
+          GenSweep<R, HET>::template stress<C>(A, a.K, out);
+          if (inside) {
+#pragma unroll
+            for (int i = 0; i < 6; ++i) a.out[F_TXX + i][o] = Storage<S>::store(out[i], a.sc[F_TXX + i]);
+          }
+        } else {
+          C out[3];
+          GenSweep<R, HET>::template velocity<C>(A, a.K, out);
+          if (inside) {
+#pragma unroll
+            for (int i = 0; i < 3; ++i) a.out[F_U + i][o] = Storage<S>::store(out[i], a.sc[F_U + i]);
+          }
+        }
+      }
+      // this warp is done with x-window plane x - R and plane-ring plane x
+      __syncwarp();
+      if (lane == 0) {
+        mbar_arrive(&xemp[(x - R - hq0) % G::NSH]);
+        mbar_arrive(&cemp[(x - xb) % G::NSC]);
+      }
     }
   }
-  if (abort_flag && tid == 0) {
-    // drain the loads this CTA issued and has not seen complete (bounded)
-    for (int pl = hwaited + 1; pl <= hissued; ++pl) {
+  __syncthreads();
+  if (abort_flag && warp == G::NCW && lane == 0) {
+    // drain: wait (bounded) for the last load issued into every slot, so that
+    // no copy is still writing this CTA's shared memory when it exits
+    for (int pl = hissued; pl > hissued - G::NSH && pl >= hq0; --pl) {
       const int q = pl - hq0;
       mbar_wait(&xbar[q % G::NSH], (unsigned)((q / G::NSH) & 1));
     }
-    for (int pl = pwaited + 1; pl <= pissued; ++pl) {
+    for (int pl = pissued; pl > pissued - G::NSC && pl >= xb; --pl) {
       const int q = pl - xb;
       mbar_wait(&cbar[q % G::NSC], (unsigned)((q / G::NSC) & 1));
     }
