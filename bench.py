@@ -145,7 +145,7 @@ def run_reference(args, rank):
     val, cores, secs = cpu_oracle(n, args.space_order, steps)
     line = {
         'impl': 'reference', 'metric': METRIC, 'value': val, 'unit': UNIT,
-        'n_gpus': 0, 'steps': steps, 'warmup': 0, 'ms_per_step': secs * 1e3 / steps,
+        'n_gpus': args.gpus, 'steps': steps, 'warmup': 0, 'ms_per_step': secs * 1e3 / steps,
         'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
         'data': 'synthetic (seeded layered medium, Ricker source)',
         'config': {'workload': 'elastic %d^3 SO%d FP32 heterogeneous + Ricker source, free surfaces' % (n, args.space_order),
@@ -171,7 +171,7 @@ def main():
     ap.add_argument('--ref-size', type=int, default=None)
     ap.add_argument('--ref-steps', type=int, default=10)
     ap.add_argument('--cpu-size', type=int, default=256)
-    ap.add_argument('--cpu-steps', type=int, default=20)
+    ap.add_argument('--cpu-steps', type=int, default=200)   # ~10 s of CPU work at 256^3
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--no-e2e', action='store_true')
     args = ap.parse_args()
