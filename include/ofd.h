@@ -137,6 +137,29 @@ int ofd_set_tuning(ofd_handle *h, int stress_variant, int velocity_variant, int 
  * whose steps are shorter than the launches they would otherwise need.
  * Results are identical to the per-kernel path. */
 int ofd_set_persistent(ofd_handle *h, int enable);
+
+/* Groups (no counterpart in the reference, which runs one model per
+ * process): many independent simulations advanced together, each phase of a
+ * step one launch over every member (8 launches per step for the whole
+ * group, captured in a two-step CUDA graph).  Members must share the space
+ * order, storage and media mode, stand at the same time level, and be large
+ * enough for the tiled sweeps (interior >= 32 along z, >= 8 along y); grids,
+ * step counts, media, sources and coefficients may differ.  The group copies
+ * the members' arguments when it is created: configure members first, and
+ * do not destroy a member before its group.  chunk_planes: x planes per
+ * sweep CTA (0: the single-handle heuristic).  ofd_group_step orders itself
+ * after work already queued on the members' streams and before work queued
+ * on them later; it advances every member's step count.  Results equal
+ * stepping each member alone. */
+typedef struct ofd_group ofd_group;
+int ofd_group_create(ofd_handle *const *members, int n, int chunk_planes, ofd_group **out);
+int ofd_group_step(ofd_group *g, int nsteps);
+/* 0 = idle, 1 = busy (non-blocking) */
+int ofd_group_query(ofd_group *g);
+/* waits, then reports OFD_ETIMEOUT if a member's bounded device wait expired */
+int ofd_group_sync(ofd_group *g);
+int ofd_group_destroy(ofd_group *g);
+
 /* completed steps; the newest level is steps % 2 */
 int ofd_get_step(ofd_handle *h, long *steps);
 int ofd_set_step(ofd_handle *h, long steps);

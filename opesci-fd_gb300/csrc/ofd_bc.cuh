@@ -329,4 +329,70 @@ __global__ void __launch_bounds__(256) velocity_bc_merged_kernel(BcArgs<S> a, S 
   }
 }
 
+// ------------------------------------------------------- grouped launches
+// One launch per face normal covers the ghost work of every member of a
+// group: each member owns a contiguous range of the launch's 32 x 8 blocks
+// (its own face grid, flattened), found by binary search.
+template <typename S>
+struct GroupBc {
+  BcArgs<S> a;
+  int begin[3];        // first block of this member in the launch for face normal d
+  int bx[3], by[3];    // the member's face grid for face normal d
+  // point source and step counter (velocity ghosts, face normal 0)
+  S *txx, *tyy, *tzz;
+  long src_off;        // -1: no source
+  const float *w;
+  int nt;
+  long *step;
+  float s0, s1, s2;
+};
+
+template <typename S>
+__device__ __forceinline__ int group_bc_member(const GroupBc<S> *tab, int n, int d) {
+  __shared__ int s_member;
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (tab[mid].begin[d] <= (int)blockIdx.x) lo = mid;
+      else hi = mid - 1;
+    }
+    s_member = lo;
+  }
+  __syncthreads();
+  return s_member;
+}
+
+// blockIdx.x -> member; within the member z = field(0..5)*2 + side
+template <int R, typename S>
+__global__ void __launch_bounds__(256) stress_bc_group_kernel(const GroupBc<S> *__restrict__ tab, int n, int d) {
+  const GroupBc<S> &e = tab[group_bc_member(tab, n, d)];
+  const int local = (int)blockIdx.x - e.begin[d];
+  const int per = e.bx[d] * e.by[d];
+  const int z = local / per, r = local - z * per;
+  const int i2 = (r % e.bx[d]) * 32 + threadIdx.x;
+  const int i1 = (r / e.bx[d]) * 8 + threadIdx.y;
+  stress_bc_point<R, S, false>(e.a, d, i1, i2, z >> 1, z & 1);
+}
+
+template <int R, typename S>
+__global__ void __launch_bounds__(256) velocity_bc_group_kernel(const GroupBc<S> *__restrict__ tab, int n, int d) {
+  const GroupBc<S> &e = tab[group_bc_member(tab, n, d)];
+  const int local = (int)blockIdx.x - e.begin[d];
+  const int i2 = (local % e.bx[d]) * 32 + threadIdx.x;
+  const int i1 = (local / e.bx[d]) * 8 + threadIdx.y;
+  velocity_bc_merged_point<R, S, false>(e.a, d, i1, i2);
+  if (d == 0 && local == 0 && threadIdx.x == 0 && threadIdx.y == 0 && e.step != nullptr) {
+    const long st = *e.step;
+    if (e.src_off >= 0 && st < e.nt) {
+      const float v = e.w[st] / 3;
+      const long o = e.src_off;
+      e.txx[o] = Storage<S>::store(Storage<S>::load(e.txx[o], 1.f / e.s0) - v, e.s0);
+      e.tyy[o] = Storage<S>::store(Storage<S>::load(e.tyy[o], 1.f / e.s1) - v, e.s1);
+      e.tzz[o] = Storage<S>::store(Storage<S>::load(e.tzz[o], 1.f / e.s2) - v, e.s2);
+    }
+    *e.step = st + 1;
+  }
+}
+
 }  // namespace ofd

@@ -3,6 +3,9 @@
 // ofd_inst_*.cu file instantiates Impl<R, S> for one storage type so the
 // variants compile in parallel.
 #pragma once
+#include <algorithm>
+#include <cstring>
+#include <vector>
 #include "ofd_common.cuh"
 #include "ofd_sweep_plain.cuh"
 #include "ofd_sweep_tiled.cuh"
@@ -40,6 +43,10 @@ struct DevState {
   float Ks[OFD_MAX_K], Kv[OFD_MAX_K];
 };
 
+struct GroupPlanBase {
+  virtual ~GroupPlanBase() {}
+};
+
 // Optional per-kernel-class events of a profiled step: ev[2k], ev[2k+1]
 // bracket class k (0 stress sweep, 1 stress ghosts, 2 velocity sweep,
 // 3 velocity ghosts + source).
@@ -64,6 +71,18 @@ struct Backend {
   virtual int step_persistent(const DevState &s, int p0, int nsteps, cudaStream_t st) = 0;
   // literal-table sizes of the generated expressions for media mode het
   virtual int table_size(int het, int stress) const = 0;
+  // Grouped stepping: device tables of the members' arguments (all members
+  // share this backend's space order and storage, and one media mode), and
+  // one step of every member in 8 grouped launches.  chunk_planes: x chunk
+  // length of the members' sweep CTAs.  The tables are allocated and filled
+  // in stream order on st (no device-wide synchronisation) and freed the
+  // same way when the plan is deleted.  group_build returns nullptr and sets
+  // *cuda_err on a CUDA failure.
+  virtual GroupPlanBase *group_build(const DevState *const *members, int n, int chunk_planes, cudaStream_t st,
+                                     cudaError_t *cuda_err) = 0;
+  virtual void group_step(GroupPlanBase *plan, int t0, cudaStream_t st) = 0;
+  // the handle's sweeps can run tiled (a group member must)
+  virtual bool tiled_ok(const DevState &s) const = 0;
 };
 
 Backend *make_backend_f32(int R);
@@ -372,6 +391,193 @@ struct Impl : Backend {
     cudaMemsetAsync(s.d_bar, 0, 2 * sizeof(unsigned), st);
     return (int)cudaLaunchCooperativeKernel(kern, dim3(blocks), dim3(256), args, 0, st);
   }
+
+  // device tables of a group: sweeps [stress][t0], ghosts [t0]
+  struct Plan : GroupPlanBase {
+    cudaStream_t st = nullptr;
+    int n = 0, het = 0;
+    GroupSweep<S> *sw[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    int sw_ctas[2][2] = {{0, 0}, {0, 0}};
+    GroupBc<S> *sbc[2] = {nullptr, nullptr}, *vbc[2] = {nullptr, nullptr};
+    int sbc_blocks[3] = {0, 0, 0}, vbc_blocks[3] = {0, 0, 0};
+    bool kd[2] = {false, false};   // [stress]: literal tables follow KMap (register-held literals)
+    std::vector<void *> raw;   // allocations (tables start 128-byte aligned inside them)
+    // stream-ordered copy of a host table to a new 128-byte aligned device table
+    template <typename T>
+    cudaError_t upload(T **dst, const T *src, int count) {
+      void *p = nullptr;
+      cudaError_t e = cudaMallocAsync(&p, sizeof(T) * count + 128, st);
+      if (e != cudaSuccess) return e;
+      raw.push_back(p);
+      *dst = (T *)(((uintptr_t)p + 127) & ~(uintptr_t)127);
+      // pageable source: the copy is staged before the call returns
+      return cudaMemcpyAsync(*dst, src, sizeof(T) * count, cudaMemcpyHostToDevice, st);
+    }
+    ~Plan() override {
+      for (void *p : raw) cudaFreeAsync(p, st);
+    }
+  };
+
+  template <int HET, bool STRESS>
+  cudaError_t build_sweep_table(const DevState *const *m, int n, int t0, int chunk_planes, Plan *pl) {
+    std::vector<GroupSweep<S>> tab(n);
+    std::vector<int> order(n), len(n);
+    for (int i = 0; i < n; ++i) {
+      tab[i].a = sweep_args(*m[i], t0, STRESS);
+      int tiles, chunks;
+      tiled_params<R, S, HET, STRESS>(tab[i].a, m[i]->tiled, t0, chunk_planes, tab[i].p, &tiles, &chunks);
+      tab[i].tiles = tiles;
+      tab[i].cta_begin = tiles * chunks;   // CTA count for now
+      len[i] = tab[i].p.chunk;
+      order[i] = i;
+    }
+    // longest CTAs first, so that the short ones fill the last wave
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return len[x] > len[y]; });
+    std::vector<GroupSweep<S>> sorted(n);
+    int total = 0;
+    for (int i = 0; i < n; ++i) {
+      sorted[i] = tab[order[i]];
+      const int c = sorted[i].cta_begin;
+      sorted[i].cta_begin = total;
+      total += c;
+    }
+    pl->sw_ctas[STRESS ? 1 : 0][t0] = total;
+    return pl->upload(&pl->sw[STRESS ? 1 : 0][t0], sorted.data(), n);
+  }
+
+  // Default x chunk of a group: the longest of 128, 112, ..., 16 planes that
+  // still gives the whole launch ~8 waves of 152 SMs x 2 CTAs (long chunks
+  // fetch fewer halo planes; enough CTAs keep every SM busy).
+  static int group_chunk(const DevState *const *m, int n) {
+    const long want = 152L * 2 * 8;
+    for (int L = 128; L > 16; L -= 16) {
+      long ctas = 0;
+      for (int j = 0; j < n; ++j) {
+        const Geom &g = m[j]->g;
+        const long tiles = (long)((g.n3 - 2 * g.m + TZ - 1) / TZ) * ((g.n2 - 2 * g.m + tile_rows(R) - 1) / tile_rows(R));
+        ctas += tiles * ((g.n1 - 2 * g.m + L - 1) / L);
+      }
+      if (ctas >= want) return L;
+    }
+    return 16;
+  }
+
+  // every member's table of this sweep repeats its values as KMap says
+  template <bool STRESS>
+  static bool tables_follow_kmap(const DevState *const *m, int n) {
+    if constexpr (KMap<R, STRESS>::ok) {
+      constexpr int NK = KMap<R, STRESS>::NK;
+      for (int j = 0; j < n; ++j) {
+        const float *K = STRESS ? m[j]->Ks : m[j]->Kv;
+        if ((STRESS ? m[j]->nks : m[j]->nkv) != NK) return false;
+        for (int i = 0; i < NK; ++i) {
+          int f = 0;
+          while (KMap<R, STRESS>::at(f) != KMap<R, STRESS>::at(i)) ++f;
+          if (std::memcmp(&K[i], &K[f], sizeof(float)) != 0) return false;
+        }
+      }
+      return true;
+    }
+    return false;
+  }
+
+  GroupPlanBase *group_build(const DevState *const *m, int n, int chunk_planes, cudaStream_t st,
+                             cudaError_t *cuda_err) override {
+    Plan *pl = new Plan();
+    pl->st = st;
+    pl->n = n;
+    pl->het = m[0]->het;
+    if (pl->het) {
+      pl->kd[1] = tables_follow_kmap<true>(m, n);
+      pl->kd[0] = tables_follow_kmap<false>(m, n);
+    }
+    if (chunk_planes <= 0) chunk_planes = group_chunk(m, n);
+    cudaError_t e = cudaSuccess;
+    for (int t0 = 0; t0 < 2 && e == cudaSuccess; ++t0) {
+      if (pl->het) {
+        e = build_sweep_table<1, true>(m, n, t0, chunk_planes, pl);
+        if (e == cudaSuccess) e = build_sweep_table<1, false>(m, n, t0, chunk_planes, pl);
+      } else {
+        e = build_sweep_table<0, true>(m, n, t0, chunk_planes, pl);
+        if (e == cudaSuccess) e = build_sweep_table<0, false>(m, n, t0, chunk_planes, pl);
+      }
+    }
+    for (int t0 = 0; t0 < 2 && e == cudaSuccess; ++t0) {
+      const int t1 = 1 - t0;
+      std::vector<GroupBc<S>> stab(n), vtab(n);
+      int sb[3] = {0, 0, 0}, vb[3] = {0, 0, 0};
+      for (int i = 0; i < n; ++i) {
+        const DevState &s = *m[i];
+        stab[i].a = bc_args(s, t1, t0, s.legacy ? 0 : 1);
+        vtab[i].a = bc_args(s, t1, t1, 0);
+        for (int d = 0; d < 3; ++d) {
+          const dim3 fg = face_grid(s.g, d, 1);
+          stab[i].bx[d] = vtab[i].bx[d] = (int)fg.x;
+          stab[i].by[d] = vtab[i].by[d] = (int)fg.y;
+          stab[i].begin[d] = sb[d];
+          vtab[i].begin[d] = vb[d];
+          sb[d] += (int)(fg.x * fg.y) * 12;
+          vb[d] += (int)(fg.x * fg.y);
+        }
+        stab[i].step = nullptr;
+        stab[i].src_off = -1;
+        vtab[i].txx = fp(s, F_TXX, t1);
+        vtab[i].tyy = fp(s, F_TYY, t1);
+        vtab[i].tzz = fp(s, F_TZZ, t1);
+        vtab[i].src_off = s.src_off;
+        vtab[i].w = s.d_wav;
+        vtab[i].nt = s.nt;
+        vtab[i].step = s.d_step;
+        vtab[i].s0 = s.scale[F_TXX];
+        vtab[i].s1 = s.scale[F_TYY];
+        vtab[i].s2 = s.scale[F_TZZ];
+      }
+      for (int d = 0; d < 3; ++d) {
+        pl->sbc_blocks[d] = sb[d];
+        pl->vbc_blocks[d] = vb[d];
+      }
+      e = pl->upload(&pl->sbc[t0], stab.data(), n);
+      if (e == cudaSuccess) e = pl->upload(&pl->vbc[t0], vtab.data(), n);
+    }
+    if (e != cudaSuccess) {
+      delete pl;
+      *cuda_err = e;
+      return nullptr;
+    }
+    return pl;
+  }
+
+  void group_step(GroupPlanBase *base, int t0, cudaStream_t st) override {
+    Plan *pl = static_cast<Plan *>(base);
+    const int n = pl->n;
+    auto launch = [&](auto kern, int threads, int smem, int k) {
+      kern<<<pl->sw_ctas[k][t0], threads, smem, st>>>(pl->sw[k][t0], n);
+    };
+    auto sweep = [&](bool stress) {
+      const int k = stress ? 1 : 0;
+      if (pl->het) {
+        typedef TiledCfg<R, S, 1, true> GS;
+        typedef TiledCfg<R, S, 1, false> GV;
+        if (stress && pl->kd[1]) launch(sweep_tiled_group<R, S, 1, true, true>, GS::THREADS, GS::SMEM, k);
+        else if (stress) launch(sweep_tiled_group<R, S, 1, true, false>, GS::THREADS, GS::SMEM, k);
+        else if (pl->kd[0]) launch(sweep_tiled_group<R, S, 1, false, true>, GV::THREADS, GV::SMEM, k);
+        else launch(sweep_tiled_group<R, S, 1, false, false>, GV::THREADS, GV::SMEM, k);
+      } else {
+        typedef TiledCfg<R, S, 0, true> GS;
+        typedef TiledCfg<R, S, 0, false> GV;
+        if (stress) launch(sweep_tiled_group<R, S, 0, true, false>, GS::THREADS, GS::SMEM, k);
+        else launch(sweep_tiled_group<R, S, 0, false, false>, GV::THREADS, GV::SMEM, k);
+      }
+    };
+    sweep(true);
+    for (int d = 0; d < 3; ++d)
+      stress_bc_group_kernel<R, S><<<pl->sbc_blocks[d], dim3(32, 8), 0, st>>>(pl->sbc[t0], n, d);
+    sweep(false);
+    for (int d = 0; d < 3; ++d)
+      velocity_bc_group_kernel<R, S><<<pl->vbc_blocks[d], dim3(32, 8), 0, st>>>(pl->vbc[t0], n, d);
+  }
+
+  bool tiled_ok(const DevState &s) const override { return s.tiled.maps && tiled_supported<R, S>(s.g); }
 
   int table_size(int het, int stress) const override {
     if (het) return stress ? GenSweep<R, 1>::NK_STRESS : GenSweep<R, 1>::NK_VELOCITY;

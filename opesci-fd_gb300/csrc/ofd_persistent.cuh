@@ -107,7 +107,7 @@ __global__ void __launch_bounds__(256) persistent_steps_kernel(const __grid_cons
         const long o = (long)x * g.plane + (long)y * g.P + z;
         CoherentAcc<S> A{sa, o};
         C out[6];
-        GenSweep<R, HET>::template stress<C>(A, sa.K, out);
+        GenSweep<R, HET>::template stress<C>(A, (const float *)sa.K, out);
 #pragma unroll
         for (int f = 0; f < 6; ++f) sa.out[F_TXX + f][o] = Storage<S>::store(out[f], sa.sc[F_TXX + f]);
       }
@@ -139,7 +139,7 @@ __global__ void __launch_bounds__(256) persistent_steps_kernel(const __grid_cons
         const long o = (long)x * g.plane + (long)y * g.P + z;
         CoherentAcc<S> A{va, o};
         C out[3];
-        GenSweep<R, HET>::template velocity<C>(A, va.K, out);
+        GenSweep<R, HET>::template velocity<C>(A, (const float *)va.K, out);
 #pragma unroll
         for (int f = 0; f < 3; ++f) va.out[F_U + f][o] = Storage<S>::store(out[f], va.sc[F_U + f]);
       }

@@ -666,6 +666,132 @@ int ofd_step_graph(ofd_handle *h, int nsteps) {
   return OFD_OK;
 }
 
+// ------------------------------------------------------------- groups
+
+struct ofd_group {
+  std::vector<ofd_handle *> members;
+  GroupPlanBase *plan = nullptr;
+  Backend *be = nullptr;            // members[0]'s backend (same R and storage for all)
+  cudaStream_t stream = nullptr;
+  cudaEvent_t done = nullptr;       // group work finished (member streams wait on it)
+  std::vector<cudaEvent_t> ready;   // member work finished (the group waits on it)
+  cudaGraphExec_t graph2[2] = {nullptr, nullptr};
+  long steps = 0;                   // members' common step count parity source
+};
+
+int ofd_group_destroy(ofd_group *g) {
+  if (!g) return OFD_OK;
+  if (g->stream) cudaStreamSynchronize(g->stream);
+  for (int p = 0; p < 2; ++p)
+    if (g->graph2[p]) cudaGraphExecDestroy(g->graph2[p]);
+  delete g->plan;
+  for (cudaEvent_t e : g->ready) cudaEventDestroy(e);
+  if (g->done) cudaEventDestroy(g->done);
+  if (g->stream) cudaStreamDestroy(g->stream);
+  delete g;
+  return OFD_OK;
+}
+
+int ofd_group_create(ofd_handle *const *hs, int n, int chunk_planes, ofd_group **out) {
+  if (!hs || !out || n <= 0) return fail(OFD_EINVAL, "null argument or empty group");
+  *out = nullptr;
+  ofd_handle *h0 = hs[0];
+  if (!h0) return fail(OFD_EINVAL, "null member 0");
+  for (int i = 0; i < n; ++i) {
+    ofd_handle *h = hs[i];
+    if (!h) return fail(OFD_EINVAL, "null member %d", i);
+    if (h->device != h0->device) return fail(OFD_EINVAL, "member %d is on another device", i);
+    if (h->s.R != h0->s.R || h->s.storage != h0->s.storage)
+      return fail(OFD_EINVAL, "member %d has another space order or storage than member 0", i);
+    if (h->s.nks == 0) return fail(OFD_ESTATE, "member %d: ofd_set_coefficients has not been called", i);
+    if (h->s.het != h0->s.het) return fail(OFD_EINVAL, "member %d has another media mode than member 0", i);
+    if ((h->steps & 1) != (h0->steps & 1)) return fail(OFD_EINVAL, "member %d is at another time level", i);
+    if (!h->be->tiled_ok(h->s)) return fail(OFD_EINVAL, "member %d cannot use the tiled sweeps (grid too small)", i);
+    for (int j = 0; j < i; ++j)
+      if (hs[j] == h) return fail(OFD_EINVAL, "member %d appears twice", i);
+  }
+  ofd_group *g = new ofd_group();
+  g->members.assign(hs, hs + n);
+  g->be = h0->be;
+  g->steps = h0->steps;
+  cudaError_t e = cudaSetDevice(h0->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g->done, cudaEventDisableTiming);
+  g->ready.resize(n, nullptr);
+  for (int i = 0; i < n && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&g->ready[i], cudaEventDisableTiming);
+  if (e == cudaSuccess) {
+    std::vector<const DevState *> ms(n);
+    for (int i = 0; i < n; ++i) ms[i] = &hs[i]->s;
+    g->plan = g->be->group_build(ms.data(), n, chunk_planes, g->stream, &e);
+  }
+  if (e != cudaSuccess || !g->plan) {
+    ofd_group_destroy(g);
+    return fail(OFD_ECUDA, "group setup failed: %s", cudaGetErrorString(e));
+  }
+  *out = g;
+  return OFD_OK;
+}
+
+int ofd_group_step(ofd_group *g, int nsteps) {
+  if (!g) return fail(OFD_EINVAL, "null group");
+  if (nsteps < 0) return fail(OFD_EINVAL, "nsteps < 0");
+  if (nsteps == 0) return OFD_OK;
+  const int n = (int)g->members.size();
+  // members' earlier work (uploads, own steps) comes first
+  for (int i = 0; i < n; ++i) {
+    OFD_CUDA(cudaEventRecord(g->ready[i], g->members[i]->stream));
+    OFD_CUDA(cudaStreamWaitEvent(g->stream, g->ready[i], 0));
+  }
+  int done = 0;
+  while (nsteps - done >= 2) {
+    const int p = (int)(g->steps & 1);
+    if (!g->graph2[p]) {
+      cudaGraph_t gr = nullptr;
+      OFD_CUDA(cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal));
+      g->be->group_step(g->plan, p, g->stream);
+      g->be->group_step(g->plan, 1 - p, g->stream);
+      cudaError_t e = cudaStreamEndCapture(g->stream, &gr);
+      if (e != cudaSuccess) return fail(OFD_ECUDA, "group graph capture failed: %s", cudaGetErrorString(e));
+      e = cudaGraphInstantiate(&g->graph2[p], gr, 0);
+      cudaGraphDestroy(gr);
+      if (e != cudaSuccess) return fail(OFD_ECUDA, "group graph instantiation failed: %s", cudaGetErrorString(e));
+    }
+    OFD_CUDA(cudaGraphLaunch(g->graph2[p], g->stream));
+    g->steps += 2;
+    done += 2;
+  }
+  if (done < nsteps) {
+    g->be->group_step(g->plan, (int)(g->steps & 1), g->stream);
+    g->steps += 1;
+  }
+  OFD_CUDA(cudaGetLastError());
+  // later work on a member's own stream comes after the group's
+  OFD_CUDA(cudaEventRecord(g->done, g->stream));
+  for (int i = 0; i < n; ++i) {
+    OFD_CUDA(cudaStreamWaitEvent(g->members[i]->stream, g->done, 0));
+    g->members[i]->steps += nsteps;
+  }
+  return OFD_OK;
+}
+
+int ofd_group_query(ofd_group *g) {
+  if (!g) return fail(OFD_EINVAL, "null group");
+  const cudaError_t e = cudaStreamQuery(g->stream);
+  if (e == cudaSuccess) return 0;
+  if (e == cudaErrorNotReady) return 1;
+  return fail(OFD_ECUDA, "cudaStreamQuery: %s", cudaGetErrorString(e));
+}
+
+int ofd_group_sync(ofd_group *g) {
+  if (!g) return fail(OFD_EINVAL, "null group");
+  OFD_CUDA(cudaStreamSynchronize(g->stream));
+  for (ofd_handle *h : g->members) {
+    const int rc = check_err_word(h);
+    if (rc) return rc;
+  }
+  return OFD_OK;
+}
+
 int ofd_query(ofd_handle *h) {
   if (!h) return fail(OFD_EINVAL, "null handle");
   const cudaError_t e = cudaStreamQuery(h->stream);

@@ -48,7 +48,7 @@ __global__ void __launch_bounds__(256) stress_plain(const __grid_constant__ Swee
     const long o = (long)x * g.plane + (long)y * g.P + z;
     PlainAcc<S> A{a, o};
     C out[6];
-    GenSweep<R, HET>::template stress<C>(A, a.K, out);
+    GenSweep<R, HET>::template stress<C>(A, (const float *)a.K, out);
 #pragma unroll
     for (int i = 0; i < 6; ++i) a.out[F_TXX + i][o] = Storage<S>::store(out[i], a.sc[F_TXX + i]);
   }
@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(256) velocity_plain(const __grid_constant__ Sw
     const long o = (long)x * g.plane + (long)y * g.P + z;
     PlainAcc<S> A{a, o};
     C out[3];
-    GenSweep<R, HET>::template velocity<C>(A, a.K, out);
+    GenSweep<R, HET>::template velocity<C>(A, (const float *)a.K, out);
 #pragma unroll
     for (int i = 0; i < 3; ++i) a.out[F_U + i][o] = Storage<S>::store(out[i], a.sc[F_U + i]);
   }

@@ -32,6 +32,10 @@ constexpr int TZ = 64;          // tile width along z (two 32-lane passes)
 // tile height along y (one warp per row).  Eight rows let two CTAs share an SM
 // (measured faster than one CTA of sixteen rows, despite the extra halo rows)
 __host__ __device__ constexpr int tile_rows(int) { return 8; }
+// consumer warps per tile row: one warp covering the row's 64 z points in two
+// 32-lane halves, or (space order >= 6, whose rings leave room for one CTA per
+// SM) two warps of one point per lane, doubling the warps that hide latency
+__host__ __device__ constexpr int row_warps(int R) { return R >= 3 ? 2 : 1; }
 
 template <typename S> struct ZHalo { static constexpr int v = (int)(16 / sizeof(S)) >= 4 ? (int)(16 / sizeof(S)) : 4; };
 
@@ -145,8 +149,9 @@ __host__ __device__ constexpr int round128(int b) { return (b + 127) / 128 * 128
 template <int R, typename S, int HET, bool STRESS>
 struct TiledCfg {
   static constexpr int TY = tile_rows(R);
-  static constexpr int NCW = TY;                           // consumer warps (one per row)
-  static constexpr int THREADS = 32 * (TY + 1);            // + one producer warp
+  static constexpr int ZW = row_warps(R);                  // consumer warps per tile row
+  static constexpr int NCW = TY * ZW;                      // consumer warps
+  static constexpr int THREADS = 32 * (NCW + 1);           // + one producer warp
   static constexpr int ZH = ZHalo<S>::v;                  // z halo, rounded to 16 B
   static constexpr int HW = TZ + 2 * ZH;                   // halo box width
   static constexpr int HH = TY + 2 * R;                    // halo box height
@@ -221,14 +226,30 @@ struct TiledAcc {
   }
 };
 
-template <int R> struct TiledThreads { static constexpr int v = 32 * (tile_rows(R) + 1); };
+template <int R> struct TiledThreads { static constexpr int v = 32 * (tile_rows(R) * row_warps(R) + 1); };
+// resident CTAs per SM the register budget is sized for: space order >= 6
+// keeps one CTA per SM (its rings fill shared memory), so tell ptxas it may
+// use the whole register file rather than spill
+template <int R> struct TiledMinBlocks { static constexpr int v = R >= 3 ? 1 : 0; };
 
-template <int R, typename S, int HET, bool STRESS>
-__global__ void __launch_bounds__(TiledThreads<R>::v)
-sweep_tiled(const __grid_constant__ SweepArgs<S> a, const __grid_constant__ TiledParams p) {
+// The literal table of a heterogeneous expression held as its few distinct
+// values (KMap): v[u] is the value of every literal with index map u.  The
+// generated code indexes K with constants, so each K[i] becomes a register.
+template <int R, bool STRESS>
+struct KRegs {
+  float v[KMap<R, STRESS>::NU];
+  __device__ __forceinline__ float operator[](int i) const { return v[KMap<R, STRESS>::at(i)]; }
+};
+
+// One CTA's work: tile `tile` (z fastest) of the 64 x 8 tiling, x chunk
+// `chunk`.  a and p live in kernel parameters (single-handle launch) or in a
+// device table (grouped launch); K is the literal table (a pointer, or
+// KRegs).
+template <int R, typename S, int HET, bool STRESS, class KT>
+__device__ __forceinline__ void sweep_tile(const SweepArgs<S> &a, const TiledParams &p, int tile, int chunk,
+                                           const KT &K, unsigned char *smem_raw) {
   typedef TiledCfg<R, S, HET, STRESS> G;
   typedef typename Storage<S>::C C;
-  extern __shared__ unsigned char smem_raw[];
   unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127);
   unsigned char *xring = smem;
   unsigned char *cring = smem + G::XRING;
@@ -240,9 +261,9 @@ sweep_tiled(const __grid_constant__ SweepArgs<S> a, const __grid_constant__ Tile
 
   const Geom &g = a.g;
   constexpr int TY = G::TY;
-  const int tz = blockIdx.x % p.ntz, ty = blockIdx.x / p.ntz;
+  const int tz = tile % p.ntz, ty = tile / p.ntz;
   const int z0 = g.m + tz * TZ, y0 = g.m + ty * TY;
-  const int xb = g.m + blockIdx.y * p.chunk;
+  const int xb = g.m + chunk * p.chunk;
   const int xe = min(xb + p.chunk, g.n1 - g.m);
   if (xb >= xe) return;
   const int hq0 = xb - R;          // plane of x-window ring q = 0
@@ -271,7 +292,7 @@ sweep_tiled(const __grid_constant__ SweepArgs<S> a, const __grid_constant__ Tile
     for (int i = 0; i < G::NMF; ++i) tma_load_3d(st + G::moff(i), &p.mmap[i], bar, zc, y0, plane);
   };
 
-  // Warp specialisation: warps 0..NCW-1 compute one row each; warp NCW is
+  // Warp specialisation: warps 0..NCW-1 compute (ZW per tile row); warp NCW is
   // the producer, whose lane 0 issues every TMA load.  A slot is refilled
   // once all consumer warps have released it (empty barrier, NCW arrivals),
   // so consumers never wait on each other, only on their data.
@@ -314,7 +335,7 @@ sweep_tiled(const __grid_constant__ SweepArgs<S> a, const __grid_constant__ Tile
       }
     }
   } else {
-    const int yl = warp;
+    const int yl = warp / G::ZW, zpart = warp % G::ZW;
     const int y = y0 + yl;
     int hwaited = hq0 - 1;   // last x-window plane waited for
     for (int x = xb; x < xe; ++x) {
@@ -342,8 +363,8 @@ sweep_tiled(const __grid_constant__ SweepArgs<S> a, const __grid_constant__ Tile
       A.cs = cring + ((x - xb) % G::NSC) * G::CSTAGE;
       A.inv = a.inv;
 #pragma unroll
-      for (int half = 0; half < 2; ++half) {
-        const int zl = lane + 32 * half;
+      for (int half = 0; half < 2 / G::ZW; ++half) {
+        const int zl = lane + 32 * (zpart + half);
         const int z = z0 + zl;
         A.hpos = (yl + R) * G::HW + zl + G::ZH;
         A.ppos = yl * TZ + zl;
@@ -351,14 +372,14 @@ sweep_tiled(const __grid_constant__ SweepArgs<S> a, const __grid_constant__ Tile
         const bool inside = (z < g.n3 - g.m) && (y < g.n2 - g.m);
         if (STRESS) {
           C out[6];
-          GenSweep<R, HET>::template stress<C>(A, a.K, out);
+          GenSweep<R, HET>::template stress<C>(A, K, out);
           if (inside) {
 #pragma unroll
             for (int i = 0; i < 6; ++i) a.out[F_TXX + i][o] = Storage<S>::store(out[i], a.sc[F_TXX + i]);
           }
         } else {
           C out[3];
-          GenSweep<R, HET>::template velocity<C>(A, a.K, out);
+          GenSweep<R, HET>::template velocity<C>(A, K, out);
           if (inside) {
 #pragma unroll
             for (int i = 0; i < 3; ++i) a.out[F_U + i][o] = Storage<S>::store(out[i], a.sc[F_U + i]);
@@ -388,6 +409,76 @@ sweep_tiled(const __grid_constant__ SweepArgs<S> a, const __grid_constant__ Tile
   }
 }
 
+template <int R, typename S, int HET, bool STRESS>
+__global__ void __launch_bounds__(TiledThreads<R>::v, TiledMinBlocks<R>::v)
+sweep_tiled(const __grid_constant__ SweepArgs<S> a, const __grid_constant__ TiledParams p) {
+  extern __shared__ unsigned char smem_raw[];
+  sweep_tile<R, S, HET, STRESS>(a, p, blockIdx.x, blockIdx.y, (const float *)a.K, smem_raw);
+}
+
+// One member of a grouped sweep launch: its arguments, descriptors and the
+// range of the launch's CTAs that work on it.
+template <typename S>
+struct GroupSweep {
+  TiledParams p;        // first: CUtensorMap members need 64-byte alignment
+  SweepArgs<S> a;
+  int cta_begin;        // first CTA of this member
+  int tiles;            // tiles of this member (CTAs = tiles x chunks)
+};
+
+// Grouped sweep: CTA blockIdx.x works on the member whose range holds it
+// (binary search over the table, sorted by cta_begin).  The descriptors were
+// copied to global memory by the host before the launch; the producer lane
+// orders them for the tensor-map proxy before its first load.  KD: the
+// members' literal tables follow KMap (checked on the host), and each thread
+// holds the distinct values in registers instead of reading the table from
+// global memory at every use.
+template <int R, typename S, int HET, bool STRESS, bool KD>
+__global__ void __launch_bounds__(TiledThreads<R>::v, TiledMinBlocks<R>::v)
+sweep_tiled_group(const GroupSweep<S> *__restrict__ tab, int n) {
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ int s_member;
+  typedef TiledCfg<R, S, HET, STRESS> G;
+  if (threadIdx.x == 0) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (tab[mid].cta_begin <= (int)blockIdx.x) lo = mid;
+      else hi = mid - 1;
+    }
+    s_member = lo;
+  }
+  __syncthreads();
+  const GroupSweep<S> &e = tab[s_member];
+  // descriptors must sit on 64-byte boundaries (the host aligns the table);
+  // a misplaced table is reported, never used
+  if (((uintptr_t)&e.p) & 63) {
+    if (threadIdx.x == 0) atomicExch(e.p.err, 4);
+    return;
+  }
+  if (threadIdx.x == 32 * G::NCW) {
+    const int nmaps = G::NXF + G::NH0;
+#pragma unroll 1
+    for (int i = 0; i < nmaps; ++i)
+      asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(&e.p.hmap[i]) : "memory");
+#pragma unroll 1
+    for (int i = 0; i < G::NPF; ++i)
+      asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(&e.p.pmap[i]) : "memory");
+#pragma unroll 1
+    for (int i = 0; i < G::NMF; ++i)
+      asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(&e.p.mmap[i]) : "memory");
+  }
+  const int local = (int)blockIdx.x - e.cta_begin;
+  if constexpr (KD) {
+    KRegs<R, STRESS> kr;
+#pragma unroll
+    for (int i = 0; i < KMap<R, STRESS>::NK; ++i) kr.v[KMap<R, STRESS>::at(i)] = e.a.K[i];
+    sweep_tile<R, S, HET, STRESS>(e.a, e.p, local % e.tiles, local / e.tiles, kr, smem_raw);
+  } else {
+    sweep_tile<R, S, HET, STRESS>(e.a, e.p, local % e.tiles, local / e.tiles, (const float *)e.a.K, smem_raw);
+  }
+}
+
 // ---------------------------------------------------------------- host side
 
 template <int R, typename S, int HET, bool STRESS>
@@ -403,12 +494,15 @@ bool tiled_supported(const Geom &g) {
          tiled_fits<R, S, 0, false>();
 }
 
+// Descriptors and tiling of one sweep launch; returns the CTA grid (tiles,
+// chunks).  chunk_planes > 0 forces the x chunk length (grouped launches),
+// else the chunking aims at ~8 waves (x ctx.waves) of 152 SMs.
 template <int R, typename S, int HET, bool STRESS>
-void launch_tiled(const SweepArgs<S> &a, const TiledCtx &ctx, int t0, cudaStream_t st) {
+void tiled_params(const SweepArgs<S> &a, const TiledCtx &ctx, int t0, int chunk_planes, TiledParams &p,
+                  int *tiles_out, int *chunks_out) {
   typedef TiledCfg<R, S, HET, STRESS> G;
   const TmaMaps *mp = ctx.maps;
   const Geom &g = a.g;
-  TiledParams p;
   const int t1 = 1 - t0;
   if (STRESS) {
     for (int i = 0; i < 3; ++i) p.hmap[i] = mp->halo[F_U + i][t0];
@@ -435,7 +529,18 @@ void launch_tiled(const SweepArgs<S> &a, const TiledCtx &ctx, int t0, cudaStream
   if (chunks > nx / 16) chunks = nx / 16;
   if (chunks < 1) chunks = 1;
   p.chunk = (nx + chunks - 1) / chunks;
+  if (chunk_planes > 0) p.chunk = chunk_planes < nx ? chunk_planes : nx;
   chunks = (nx + p.chunk - 1) / p.chunk;
+  *tiles_out = (int)tiles;
+  *chunks_out = chunks;
+}
+
+template <int R, typename S, int HET, bool STRESS>
+void launch_tiled(const SweepArgs<S> &a, const TiledCtx &ctx, int t0, cudaStream_t st) {
+  typedef TiledCfg<R, S, HET, STRESS> G;
+  TiledParams p;
+  int tiles, chunks;
+  tiled_params<R, S, HET, STRESS>(a, ctx, t0, 0, p, &tiles, &chunks);
   auto kern = sweep_tiled<R, S, HET, STRESS>;
   kern<<<dim3((unsigned)tiles, (unsigned)chunks), G::THREADS, G::SMEM, st>>>(a, p);
 }
@@ -444,12 +549,18 @@ void launch_tiled(const SweepArgs<S> &a, const TiledCtx &ctx, int t0, cudaStream
 // launches can later be captured in a CUDA graph.
 template <int R, typename S, int HET>
 void prepare_tiled() {
-  if (tiled_fits<R, S, HET, true>())
-    cudaFuncSetAttribute(sweep_tiled<R, S, HET, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         TiledCfg<R, S, HET, true>::SMEM);
-  if (tiled_fits<R, S, HET, false>())
-    cudaFuncSetAttribute(sweep_tiled<R, S, HET, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         TiledCfg<R, S, HET, false>::SMEM);
+  if (tiled_fits<R, S, HET, true>()) {
+    const int sm = TiledCfg<R, S, HET, true>::SMEM;
+    cudaFuncSetAttribute(sweep_tiled<R, S, HET, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    cudaFuncSetAttribute(sweep_tiled_group<R, S, HET, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    if constexpr (HET) cudaFuncSetAttribute(sweep_tiled_group<R, S, HET, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+  }
+  if (tiled_fits<R, S, HET, false>()) {
+    const int sm = TiledCfg<R, S, HET, false>::SMEM;
+    cudaFuncSetAttribute(sweep_tiled<R, S, HET, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    cudaFuncSetAttribute(sweep_tiled_group<R, S, HET, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    if constexpr (HET) cudaFuncSetAttribute(sweep_tiled_group<R, S, HET, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+  }
 }
 
 template <int R, typename S, int HET>

@@ -88,6 +88,11 @@ def load_library():
         'ofd_field_sumsq': [h, ctypes.c_int, P(ctypes.c_double)],
         'ofd_field_absmax': [h, ctypes.c_int, P(ctypes.c_double)],
         'ofd_field_view_get': [h, ctypes.c_int, ctypes.c_int, P(ofd_field_view)],
+        'ofd_group_create': [P(h), ctypes.c_int, ctypes.c_int, P(h)],
+        'ofd_group_step': [h, ctypes.c_int],
+        'ofd_group_query': [h],
+        'ofd_group_sync': [h],
+        'ofd_group_destroy': [h],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -308,3 +313,48 @@ class Simulation(object):
         f = FIELDS.index(field) if isinstance(field, str) else field
         _check(self.lib.ofd_field_view_get(self.h, f, level, ctypes.byref(v)), 'ofd_field_view_get')
         return v
+
+
+class Group(object):
+    """Simulations advanced together (ofd_group): every phase of a step is
+    one launch over all members, replayed from a captured two-step graph.
+    Members must share space order, storage and media mode and stand at the
+    same time level; create the group after configuring them (media,
+    coefficients, source), and close it before closing a member."""
+
+    def __init__(self, sims, chunk_planes=0):
+        self.lib = load_library()
+        self.sims = list(sims)
+        arr = (ctypes.c_void_p * len(self.sims))(*[s.h.value for s in self.sims])
+        self.g = ctypes.c_void_p()
+        _check(self.lib.ofd_group_create(arr, len(self.sims), int(chunk_planes), ctypes.byref(self.g)),
+               'ofd_group_create')
+
+    def step(self, n):
+        _check(self.lib.ofd_group_step(self.g, int(n)), 'ofd_group_step')
+
+    def done(self):
+        rc = self.lib.ofd_group_query(self.g)
+        if rc < 0:
+            _check(rc, 'ofd_group_query')
+        return rc == 0
+
+    def sync(self):
+        _check(self.lib.ofd_group_sync(self.g), 'ofd_group_sync')
+
+    def close(self):
+        if self.g:
+            self.lib.ofd_group_destroy(self.g)
+            self.g = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

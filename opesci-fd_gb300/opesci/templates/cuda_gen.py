@@ -167,24 +167,56 @@ def generate_headers(outdir):
             lines.append('template <> struct GenSweep<%d, %d> {' % (so // 2, het))
             lines.append('  static constexpr bool ok = true;')
             lines.append('  static constexpr int NK_STRESS = %d, NK_VELOCITY = %d;' % (len(sl), len(vl)))
-            lines.append('  template <typename C, class Acc>')
-            lines.append('  __device__ __forceinline__ static void stress(const Acc &A, const float *K, C out[6]) {')
+            lines.append('  template <typename C, class Acc, class KT>')
+            lines.append('  __device__ __forceinline__ static void stress(const Acc &A, const KT &K, C out[6]) {')
             for i, e in enumerate(se):
                 lines.append('    out[%d] = %s;' % (i, e))
             lines.append('  }')
-            lines.append('  template <typename C, class Acc>')
-            lines.append('  __device__ __forceinline__ static void velocity(const Acc &A, const float *K, C out[3]) {')
+            lines.append('  template <typename C, class Acc, class KT>')
+            lines.append('  __device__ __forceinline__ static void velocity(const Acc &A, const KT &K, C out[3]) {')
             for i, e in enumerate(ve):
                 lines.append('    out[%d] = %s;' % (i, e))
             lines.append('  }')
             lines.append('};')
             lines.append('')
+    lines += kmap_lines(sigs)
     lines.append('}  // namespace ofd')
     with open(os.path.join(outdir, 'sweeps_gen.cuh'), 'w') as f:
         f.write('\n'.join(lines) + '\n')
     with open(os.path.join(outdir, 'signatures.json'), 'w') as f:
         json.dump(sigs, f, indent=1, sort_keys=True)
     return sigs
+
+
+def kmap_lines(sigs):
+    """C++ of KMap<R, STRESS>: for the heterogeneous expressions, the index of
+    each literal among the distinct rationals of its unit table.  A table
+    K_i = r_i dt / h (isotropic spacing) has equal values wherever the r_i
+    are equal, so K can be held as those few distinct values."""
+    lines = ['// Literal index -> index among the distinct unit rationals of the',
+             '// heterogeneous expression (tables K_i = r_i dt / h repeat a few values).',
+             'template <int R, bool STRESS> struct KMap { static constexpr bool ok = false; };', '']
+    for so in (2, 4, 6, 8):
+        key = 'so%d_het' % so
+        if key not in sigs:
+            continue
+        for kind, stress in (('unit_stress', 'true'), ('unit_velocity', 'false')):
+            uniq, idx = [], []
+            for t in sigs[key][kind]:
+                q = Fraction(t)
+                if q not in uniq:
+                    uniq.append(q)
+                idx.append(uniq.index(q))
+            lines.append('template <> struct KMap<%d, %s> {' % (so // 2, stress))
+            lines.append('  static constexpr bool ok = true;')
+            lines.append('  static constexpr int NU = %d, NK = %d;' % (len(uniq), len(idx)))
+            lines.append('  __host__ __device__ static constexpr int at(int i) {')
+            lines.append('    constexpr int m[%d] = {%s};' % (len(idx), ', '.join(str(i) for i in idx)))
+            lines.append('    return m[i];')
+            lines.append('  }')
+            lines.append('};')
+            lines.append('')
+    return lines
 
 
 def prebuilt_signatures():

@@ -47,6 +47,83 @@ def test_batched_equals_one_by_one():
 
 
 @pytest.mark.gpu
+def test_grouped_equals_one_by_one():
+    """Grouped launches (one launch per phase over all shots of a space
+    order, groups rebuilt as shots finish, odd remainders) reproduce each
+    shot alone bit for bit."""
+    shots = [batch.Shot(n, so, st, seed=i, f0=10.0 + i) for i, (n, so, st) in
+             enumerate([(33, 4, 31), (48, 8, 20), (40, 4, 17), (70, 4, 12), (36, 8, 25), (64, 8, 9),
+                        (100, 4, 14), (57, 4, 31)])]
+    keep = set(range(len(shots)))
+    built = [s.build() for s in shots]
+    _, a = batch.run_one_by_one(shots, keep=keep, built=built)
+    for chunk in (0, 24):
+        _, b = batch.run_grouped(shots, keep=keep, built=built, chunk_planes=chunk)
+        for i in keep:
+            for f in runtime.FIELDS:
+                assert np.array_equal(a[i][f], b[i][f]), (chunk, i, f)
+
+
+@pytest.mark.gpu
+def test_group_of_16bit_members_and_member_streams():
+    """A group of scaled-FP16 members, with work queued on a member's own
+    stream before and after the group step, equals stepping alone."""
+    scales = [2.0 ** 30] * 3 + [2.0 ** 9] * 6
+    shots = [batch.Shot(n, 4, 14, seed=30 + i, f0=12.0) for i, n in enumerate((40, 52, 45))]
+
+    def make(s):
+        cfg, media, src, wav, ks, kv = s.build()
+        c = runtime.make_config(list(cfg.dim), 4, list(cfg.spacing), cfg.dt, list(cfg.weights), storage='f16',
+                                free_surface=list(cfg.free_surface), field_scale=scales)
+        sim = runtime.Simulation(c)
+        sim.set_coefficients(1, ks, kv)
+        sim.set_media(*media)
+        sim.set_source(src, wav)
+        return sim
+
+    alone = []
+    for s in shots:
+        sim = make(s)
+        sim.step(14)
+        sim.sync()
+        alone.append({f: sim.download(f) for f in runtime.FIELDS})
+        sim.close()
+    sims = [make(s) for s in shots]
+    sims[0].step(3)
+    for sim in sims[1:]:
+        sim.step_graph(3)
+    g = runtime.Group(sims)
+    g.step(9)
+    sims[1].step(2)          # queued on a member stream after the group
+    g.sync()
+    sims[0].step(2)
+    sims[2].step_graph(2)
+    for i, sim in enumerate(sims):
+        sim.sync()
+        assert sim.steps == 14
+        for f in runtime.FIELDS:
+            assert np.array_equal(alone[i][f], sim.download(f)), (i, f)
+    g.close()
+    for sim in sims:
+        sim.close()
+
+
+@pytest.mark.gpu
+def test_group_rejects_unfit_members():
+    a = batch.prepare(batch.Shot(40, 4, 5, seed=1, f0=10.0), tuned=False)
+    b = batch.prepare(batch.Shot(40, 8, 5, seed=2, f0=10.0), tuned=False)
+    c = batch.prepare(batch.Shot(40, 4, 5, seed=3, f0=10.0), tuned=False)
+    tiny = batch.prepare(batch.Shot(12, 4, 5, seed=4, f0=10.0), tuned=False)
+    c.step(1)
+    for members, msg in (([a, b], 'space order'), ([a, c], 'time level'), ([a, tiny], 'tiled'),
+                         ([a, a], 'twice')):
+        with pytest.raises(runtime.OFDError, match=msg):
+            runtime.Group(members)
+    for x in (a, b, c, tiny):
+        x.close()
+
+
+@pytest.mark.gpu
 def test_graph_steps_equal_plain_steps():
     s = batch.Shot(45, 4, 23, seed=5, f0=15.0)
     built = s.build()
