@@ -153,6 +153,9 @@ int ofd_set_persistent(ofd_handle *h, int enable);
  * stepping each member alone. */
 typedef struct ofd_group ofd_group;
 int ofd_group_create(ofd_handle *const *members, int n, int chunk_planes, ofd_group **out);
+/* 1 when the handle may join a group (coefficients set, grid large enough
+ * for the tiled sweeps), 0 when not, negative on error */
+int ofd_group_eligible(ofd_handle *h);
 int ofd_group_step(ofd_group *g, int nsteps);
 /* 0 = idle, 1 = busy (non-blocking) */
 int ofd_group_query(ofd_group *g);

@@ -732,6 +732,11 @@ int ofd_group_create(ofd_handle *const *hs, int n, int chunk_planes, ofd_group *
   return OFD_OK;
 }
 
+int ofd_group_eligible(ofd_handle *h) {
+  if (!h) return fail(OFD_EINVAL, "null handle");
+  return (h->s.nks > 0 && h->be->tiled_ok(h->s)) ? 1 : 0;
+}
+
 int ofd_group_step(ofd_group *g, int nsteps) {
   if (!g) return fail(OFD_EINVAL, "null group");
   if (nsteps < 0) return fail(OFD_EINVAL, "nsteps < 0");

@@ -201,9 +201,9 @@ def run_grouped(shots, budget_bytes=150e9, keep=None, built=None, chunk_planes=0
                 if not live:
                     continue
                 k = min(rem[i] for i in live)
-                g = runtime.Group([sims[i] for i in live], chunk_planes=chunk_planes)
-                g.step(k)
-                retired.append(g)
+                for g in runtime.make_groups([sims[i] for i in live], chunk_planes=chunk_planes):
+                    g.step(k)
+                    retired.append(g)
                 for i in live:
                     rem[i] -= k
         for g in retired:

@@ -90,6 +90,7 @@ def load_library():
         'ofd_field_view_get': [h, ctypes.c_int, ctypes.c_int, P(ofd_field_view)],
         'ofd_group_create': [P(h), ctypes.c_int, ctypes.c_int, P(h)],
         'ofd_group_step': [h, ctypes.c_int],
+        'ofd_group_eligible': [h],
         'ofd_group_query': [h],
         'ofd_group_sync': [h],
         'ofd_group_destroy': [h],
@@ -280,6 +281,13 @@ class Simulation(object):
     def sync(self):
         _check(self.lib.ofd_sync(self.h), 'ofd_sync')
 
+    def groupable(self):
+        """True when this simulation may join a Group (tiled sweeps apply)."""
+        rc = self.lib.ofd_group_eligible(self.h)
+        if rc < 0:
+            _check(rc, 'ofd_group_eligible')
+        return rc == 1
+
     @property
     def steps(self):
         v = ctypes.c_long()
@@ -313,6 +321,35 @@ class Simulation(object):
         f = FIELDS.index(field) if isinstance(field, str) else field
         _check(self.lib.ofd_field_view_get(self.h, f, level, ctypes.byref(v)), 'ofd_field_view_get')
         return v
+
+
+class Solo(object):
+    """A simulation stepped on its own stream, with the Group interface
+    (done/sync/close) so that drivers can mix it with groups."""
+
+    def __init__(self, sim):
+        self.sims = [sim]
+
+    def step(self, n):
+        self.sims[0].step_graph(n)
+
+    def done(self):
+        return self.sims[0].done()
+
+    def sync(self):
+        self.sims[0].sync()
+
+    def close(self):
+        pass
+
+
+def make_groups(sims, chunk_planes=0):
+    """Group and Solo objects covering ``sims`` (which share space order,
+    storage, media mode and time level): one Group of every simulation that
+    may join one, a Solo for each other."""
+    ok = [s for s in sims if s.groupable()]
+    out = [Group(ok, chunk_planes=chunk_planes)] if ok else []
+    return out + [Solo(s) for s in sims if not s.groupable()]
 
 
 class Group(object):

@@ -28,6 +28,21 @@ def test_served_results_equal_alone_results():
 
 
 @pytest.mark.gpu
+def test_grouped_server_results_equal_alone_results():
+    """Grouped continuous batching (requests of one space order, storage and
+    parity share every launch; small grids step alone) answers each request
+    with the fields it gets alone."""
+    reqs = serve.make_requests(14, 300.0, seed=11, edge_range=(24, 72), steps_range=(15, 70), fp16_fraction=0.3)
+    built = {r.id: r.shot.build() for r in reqs}
+    mix, alone = {}, {}
+    st = serve.serve_grouped(reqs, built, budget_bytes=4e9, slice_steps=6, checks=mix)
+    serve.serve_one_by_one(reqs, built, checks=alone)
+    assert serve.max_rel_diff(mix, alone) == 0.0
+    assert st['p99_s'] >= st['p50_s'] > 0
+    assert any(r.storage == 'f16' for r in reqs) and any(r.shot.n < 32 for r in reqs)
+
+
+@pytest.mark.gpu
 def test_budget_limits_admission():
     reqs = serve.make_requests(6, 1000.0, seed=2, edge_range=(40, 48), steps_range=(20, 30), fp16_fraction=0.0)
     built = {r.id: r.shot.build() for r in reqs}
