@@ -101,6 +101,18 @@ int ofd_zero_fields(ofd_handle *h);
  * (sx, sy, sz) is an array index including margins. */
 int ofd_set_source(ofd_handle *h, int sx, int sy, int sz, const float *wavelet, int nt);
 
+/* Receivers (seismograms; the reference records them in its hand-written
+ * driver, tests/src/test_ref_iso_elastic.cpp:227-270, reading positions with
+ * opesci_read_receivers, src/opesciIO.cpp:372-396).  ijk: 3*nrec array
+ * indices (x, y, z, margins included).  After every step, once its ghosts
+ * and source are applied, row (step - 1) of a device buffer
+ * traces[nt_cap][4][nrec] receives U, V, W and P = (Txx + Tyy + Tzz) / 3 of
+ * the new level; steps beyond nt_cap are not recorded.  nrec = 0 removes the
+ * receivers.  The buffer starts at zero. */
+int ofd_set_receivers(ofd_handle *h, int nrec, const int *ijk, int nt_cap);
+/* copy the whole trace buffer (nt_cap * 4 * nrec floats) to host memory */
+int ofd_get_traces(ofd_handle *h, float *host);
+
 /* Ghost cells of one level as the reference's initialise_bc does for the
  * initial level (staggeredgrid.py:866-879): stress mirrors, then velocity
  * ghosts. */

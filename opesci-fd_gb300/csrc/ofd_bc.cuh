@@ -329,6 +329,54 @@ __global__ void __launch_bounds__(256) velocity_bc_merged_kernel(BcArgs<S> a, S 
   }
 }
 
+// ------------------------------------------------------------ receivers
+// Seismogram sampling (tests/src/test_ref_iso_elastic.cpp:227-270 records
+// U, V, W and the pressure (Txx + Tyy + Tzz) / 3 at each receiver every
+// step): after a step's velocity ghosts and source, row (step counter - 1)
+// of traces[cap][4][nrec] receives the values of level t1.  Steps beyond
+// the buffer's capacity are not recorded.
+template <typename S>
+struct RecArgs {
+  const S *f[6];       // U V W Txx Tyy Tzz at level t1
+  float inv[6];        // 1 / storage scale
+  const long *rec;     // element offsets of the receivers
+  int nrec, cap;
+  float *traces;
+  const long *step;    // device step counter, already advanced
+};
+
+// COH: read through L2 only (values written by other CTAs of the same launch)
+template <bool COH, typename S>
+__device__ __forceinline__ void sample_receiver_at(const RecArgs<S> &r, long row, int i) {
+  typedef typename Storage<S>::C C;
+  const long o = r.rec[i];
+  float *t = r.traces + row * 4 * (long)r.nrec;
+  auto L = [&](int k) -> C { return (C)Storage<S>::load(ldg<COH>(&r.f[k][o]), r.inv[k]); };
+  t[i] = (float)L(0);
+  t[r.nrec + i] = (float)L(1);
+  t[2 * r.nrec + i] = (float)L(2);
+  const C p = (L(3) + L(4) + L(5)) / 3;
+  t[3 * r.nrec + i] = (float)p;
+}
+
+template <typename S>
+__device__ __forceinline__ void sample_receiver(const RecArgs<S> &r, long row, int i) {
+  sample_receiver_at<false>(r, row, i);
+}
+
+template <typename S>
+__device__ __forceinline__ void sample_receiver_coherent(const RecArgs<S> &r, long row, int i) {
+  sample_receiver_at<true>(r, row, i);
+}
+
+template <typename S>
+__global__ void receiver_sample_kernel(RecArgs<S> r) {
+  const long row = *r.step - 1;
+  if (row < 0 || row >= r.cap) return;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < r.nrec; i += gridDim.x * blockDim.x)
+    sample_receiver(r, row, i);
+}
+
 // ------------------------------------------------------- grouped launches
 // One launch per face normal covers the ghost work of every member of a
 // group: each member owns a contiguous range of the launch's 32 x 8 blocks
@@ -345,6 +393,7 @@ struct GroupBc {
   int nt;
   long *step;
   float s0, s1, s2;
+  RecArgs<S> rec;      // receivers of the member (nrec = 0: none)
 };
 
 template <typename S>
@@ -393,6 +442,16 @@ __global__ void __launch_bounds__(256) velocity_bc_group_kernel(const GroupBc<S>
     }
     *e.step = st + 1;
   }
+}
+
+// receivers of every member: block = member
+template <typename S>
+__global__ void receiver_sample_group_kernel(const GroupBc<S> *__restrict__ tab) {
+  const RecArgs<S> &r = tab[blockIdx.x].rec;
+  if (r.nrec <= 0) return;
+  const long row = *r.step - 1;
+  if (row < 0 || row >= r.cap) return;
+  for (int i = threadIdx.x; i < r.nrec; i += blockDim.x) sample_receiver(r, row, i);
 }
 
 }  // namespace ofd

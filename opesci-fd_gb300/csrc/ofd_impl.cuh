@@ -32,6 +32,11 @@ struct DevState {
   int variant;         // 0 best, 1 plain
   double *d_partial;   // reduction scratch (>= 2048 doubles)
   long *d_step;        // device step counter (graph-safe source index)
+  // receivers: element offsets (in a level) and a trace buffer
+  // traces[step][k][r], k = U V W P with P = (Txx + Tyy + Tzz) / 3
+  int nrec, rec_cap;
+  long *d_rec;
+  float *d_traces;
   TiledCtx tiled;      // TMA descriptors for the tiled sweeps
   // launch tuning (autotuner knobs): per-sweep variant 0 tiled / 1 plain,
   // target waves for the x chunking, plain-kernel block shape
@@ -311,6 +316,28 @@ struct Impl : Backend {
     }
   }
 
+  // one trace row per completed step (row = device step counter - 1)
+  void sample_receivers(const DevState &s, int t1, cudaStream_t st) {
+    if (s.nrec <= 0) return;
+    RecArgs<S> r = rec_args(s, t1);
+    receiver_sample_kernel<S><<<(s.nrec + 127) / 128, 128, 0, st>>>(r);
+  }
+
+  RecArgs<S> rec_args(const DevState &s, int t1) const {
+    RecArgs<S> r;
+    for (int i = 0; i < 6; ++i) {
+      const int f = i < 3 ? F_U + i : F_TXX + (i - 3);
+      r.f[i] = fp(s, f, t1);
+      r.inv[i] = 1.f / s.scale[f];
+    }
+    r.rec = s.d_rec;
+    r.nrec = s.nrec;
+    r.traces = s.d_traces;
+    r.cap = s.rec_cap;
+    r.step = s.d_step;
+    return r;
+  }
+
   void step(const DevState &s, int t0, cudaStream_t st, const StepEvents *ev) override {
     const int t1 = 1 - t0;
     auto rec = [&](int i) { if (ev) cudaEventRecord(ev->ev[i], st); };
@@ -325,13 +352,14 @@ struct Impl : Backend {
     rec(5);
     rec(6);
     velocity_bc(s, t1, true, st);
+    sample_receivers(s, t1, st);
     rec(7);
   }
 
   int launches_per_step(const DevState &s) const override {
     // 2 sweeps + 3 stress-ghost phases + 3 velocity-ghost phases (the first
-    // carries the source and the step counter)
-    return 2 + 3 + 3;
+    // carries the source and the step counter) + receivers, if any
+    return 2 + 3 + 3 + (s.nrec > 0 ? 1 : 0);
   }
 
   void boundary_init(const DevState &s, int level, cudaStream_t st) override {
@@ -372,6 +400,7 @@ struct Impl : Backend {
     a.ssc[2] = s.scale[F_TZZ];
     a.bar = s.d_bar;
     a.err = s.tiled.err;
+    for (int p = 0; p < 2; ++p) a.rec[p] = rec_args(s, 1 - p);
     a.nsteps = nsteps;
     a.p0 = p0;
     void *kern = s.het ? (void *)persistent_steps_kernel<R, S, 1> : (void *)persistent_steps_kernel<R, S, 0>;
@@ -401,6 +430,7 @@ struct Impl : Backend {
     GroupBc<S> *sbc[2] = {nullptr, nullptr}, *vbc[2] = {nullptr, nullptr};
     int sbc_blocks[3] = {0, 0, 0}, vbc_blocks[3] = {0, 0, 0};
     bool kd[2] = {false, false};   // [stress]: literal tables follow KMap (register-held literals)
+    bool receivers = false;        // some member records traces
     std::vector<void *> raw;   // allocations (tables start 128-byte aligned inside them)
     // stream-ordered copy of a host table to a new 128-byte aligned device table
     template <typename T>
@@ -531,6 +561,9 @@ struct Impl : Backend {
         vtab[i].s0 = s.scale[F_TXX];
         vtab[i].s1 = s.scale[F_TYY];
         vtab[i].s2 = s.scale[F_TZZ];
+        vtab[i].rec = rec_args(s, t1);
+        stab[i].rec = vtab[i].rec;
+        if (s.nrec > 0) pl->receivers = true;
       }
       for (int d = 0; d < 3; ++d) {
         pl->sbc_blocks[d] = sb[d];
@@ -575,6 +608,7 @@ struct Impl : Backend {
     sweep(false);
     for (int d = 0; d < 3; ++d)
       velocity_bc_group_kernel<R, S><<<pl->vbc_blocks[d], dim3(32, 8), 0, st>>>(pl->vbc[t0], n, d);
+    if (pl->receivers) receiver_sample_group_kernel<S><<<n, 128, 0, st>>>(pl->vbc[t0]);
   }
 
   bool tiled_ok(const DevState &s) const override { return s.tiled.maps && tiled_supported<R, S>(s.g); }

@@ -45,6 +45,7 @@ struct PersistArgs {
   int *err;
   int nsteps;
   int p0;               // parity of the first step
+  RecArgs<S> rec[2];    // receivers by parity of t0 (level t1 = 1 - p)
 };
 
 __device__ __forceinline__ unsigned long long wall_ns() {
@@ -169,6 +170,14 @@ __global__ void __launch_bounds__(256) persistent_steps_kernel(const __grid_cons
         *a.d_step = st + 1;
       }
       if (!grid_barrier(a.bar, a.err)) return;
+    }
+    // receivers read level t1, which the next step's phases do not write
+    // (they write the other level), so no barrier follows
+    const RecArgs<S> &rc = a.rec[p];
+    if (rc.nrec > 0) {
+      const long row = *(volatile long *)a.d_step - 1;
+      if (row >= 0 && row < rc.cap)
+        for (long i = gtid; i < rc.nrec; i += gstride) sample_receiver_coherent(rc, row, (int)i);
     }
   }
 }

@@ -321,6 +321,10 @@ int ofd_create(const ofd_config *cfg, ofd_handle **out) {
   h->s.persistent = 0;
   h->s.d_wav = nullptr;
   h->s.src_off = -1;
+  h->s.nrec = 0;
+  h->s.rec_cap = 0;
+  h->s.d_rec = nullptr;
+  h->s.d_traces = nullptr;
   h->s.nt = 0;
   for (int f = 0; f < NF; ++f) h->s.scale[f] = cfg->field_scale[f] > 0 ? cfg->field_scale[f] : 1.f;
   if (cfg->storage == OFD_F32 || cfg->storage == OFD_F64)
@@ -370,6 +374,8 @@ int ofd_destroy(ofd_handle *h) {
   delete h->be;
   delete h->maps;
   if (h->s.d_wav) cudaFree(h->s.d_wav);
+  if (h->s.d_rec) cudaFree(h->s.d_rec);
+  if (h->s.d_traces) cudaFree(h->s.d_traces);
   if (h->fields_raw) cudaFree(h->fields_raw);
   if (h->media_raw) cudaFree(h->media_raw);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -512,6 +518,52 @@ int ofd_set_source(ofd_handle *h, int sx, int sy, int sz, const float *wavelet, 
   h->s.nt = nt;
   h->s.src_off = (long)sx * g.plane + (long)sy * g.P + sz;
   drop_graphs(h);
+  return OFD_OK;
+}
+
+int ofd_set_receivers(ofd_handle *h, int nrec, const int *ijk, int nt_cap) {
+  if (!h) return fail(OFD_EINVAL, "null handle");
+  if (nrec < 0 || nt_cap < 0 || (nrec > 0 && (!ijk || nt_cap == 0)))
+    return fail(OFD_EINVAL, "bad receiver arguments");
+  const Geom &g = h->s.g;
+  std::vector<long> off(nrec);
+  for (int i = 0; i < nrec; ++i) {
+    const int x = ijk[3 * i], y = ijk[3 * i + 1], z = ijk[3 * i + 2];
+    if (x < 0 || x >= g.n1 || y < 0 || y >= g.n2 || z < 0 || z >= g.n3)
+      return fail(OFD_EINVAL, "receiver %d at (%d,%d,%d) outside the grid", i, x, y, z);
+    off[i] = (long)x * g.plane + (long)y * g.P + z;
+  }
+  if ((double)nt_cap * 4.0 * nrec * sizeof(float) > 64e9)
+    return fail(OFD_EINVAL, "trace buffer of %d steps x %d receivers is too large", nt_cap, nrec);
+  OFD_CUDA(cudaStreamSynchronize(h->stream));
+  if (h->s.d_rec) cudaFree(h->s.d_rec);
+  if (h->s.d_traces) cudaFree(h->s.d_traces);
+  h->s.d_rec = nullptr;
+  h->s.d_traces = nullptr;
+  h->s.nrec = 0;
+  h->s.rec_cap = 0;
+  drop_graphs(h);
+  if (nrec == 0) return OFD_OK;
+  const size_t tbytes = sizeof(float) * 4 * (size_t)nrec * nt_cap;
+  if (cudaMalloc((void **)&h->s.d_rec, sizeof(long) * nrec) != cudaSuccess ||
+      cudaMalloc((void **)&h->s.d_traces, tbytes) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(OFD_ENOMEM, "cannot allocate %zu bytes of traces", tbytes);
+  }
+  OFD_CUDA(cudaMemcpyAsync(h->s.d_rec, off.data(), sizeof(long) * nrec, cudaMemcpyHostToDevice, h->stream));
+  OFD_CUDA(cudaMemsetAsync(h->s.d_traces, 0, tbytes, h->stream));
+  OFD_CUDA(cudaStreamSynchronize(h->stream));
+  h->s.nrec = nrec;
+  h->s.rec_cap = nt_cap;
+  return OFD_OK;
+}
+
+int ofd_get_traces(ofd_handle *h, float *host) {
+  if (!h || !host) return fail(OFD_EINVAL, "null argument");
+  if (h->s.nrec == 0) return fail(OFD_ESTATE, "no receivers set");
+  const size_t tbytes = sizeof(float) * 4 * (size_t)h->s.nrec * h->s.rec_cap;
+  OFD_CUDA(cudaMemcpyAsync(host, h->s.d_traces, tbytes, cudaMemcpyDeviceToHost, h->stream));
+  OFD_CUDA(cudaStreamSynchronize(h->stream));
   return OFD_OK;
 }
 

@@ -75,6 +75,8 @@ def load_library():
         'ofd_download_field_device': [h, ctypes.c_int, ctypes.c_int, ctypes.c_void_p],
         'ofd_zero_fields': [h],
         'ofd_set_source': [h, ctypes.c_int, ctypes.c_int, ctypes.c_int, fptr, ctypes.c_int],
+        'ofd_set_receivers': [h, ctypes.c_int, P(ctypes.c_int), ctypes.c_int],
+        'ofd_get_traces': [h, fptr],
         'ofd_apply_boundary_init': [h, ctypes.c_int],
         'ofd_step': [h, ctypes.c_int],
         'ofd_step_graph': [h, ctypes.c_int],
@@ -239,6 +241,20 @@ class Simulation(object):
         w = np.ascontiguousarray(wavelet, dtype=np.float32)
         _check(self.lib.ofd_set_source(self.h, int(pos[0]), int(pos[1]), int(pos[2]), _fptr(w), len(w)),
                'ofd_set_source')
+
+    def set_receivers(self, ijk, nt_cap):
+        """Record U, V, W and P = (Txx+Tyy+Tzz)/3 at array indices ``ijk``
+        ((n, 3), margins included) after every step, for up to nt_cap steps."""
+        a = np.ascontiguousarray(np.asarray(ijk, dtype=np.int32).reshape(-1, 3))
+        self._nrec, self._rec_cap = len(a), int(nt_cap)
+        _check(self.lib.ofd_set_receivers(self.h, len(a), a.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                          int(nt_cap)), 'ofd_set_receivers')
+
+    def traces(self):
+        """Recorded traces, shape (nt_cap, 4, nrec): U, V, W, P per step."""
+        out = np.empty((self._rec_cap, 4, self._nrec), dtype=np.float32)
+        _check(self.lib.ofd_get_traces(self.h, _fptr(out)), 'ofd_get_traces')
+        return out
 
     def boundary_init(self, level=0):
         _check(self.lib.ofd_apply_boundary_init(self.h, level), 'ofd_apply_boundary_init')

@@ -19,6 +19,10 @@ arithmetic):
     the upper interior plane and in ghost formulas);
   * an optional point source, T_ii[t1][s] -= w[ti]/3 after each step, as in
     tests/src/test_ref_iso_elastic.cpp:274-290;
+  * optional receivers: after each step (ghosts and source applied) U, V, W
+    and (Txx + Tyy + Tzz)/3 of level t1 at given array indices, as the
+    reference's driver records them (test_ref_iso_elastic.cpp:227-270),
+    dumped as traces[ntsteps][4][nrec];
   * omp_get_wtime() around the time loop, FP64 error/energy sums beside the
     reference's float L2, and raw dumps of the final time level.
 """
@@ -283,7 +287,7 @@ def converge_test(grid):
     return out
 
 
-def generate(grid, legacy=False, dump_prefix=None, source=None, timer=True):
+def generate(grid, legacy=False, dump_prefix=None, source=None, timer=True, receivers=None):
     """The whole program: includes, ABI structs, opesci_execute,
     opesci_convergence, opesci_free and main (regular3d_tmpl.py:7-134)."""
     c = _Code()
@@ -302,6 +306,9 @@ def generate(grid, legacy=False, dump_prefix=None, source=None, timer=True):
     if source is not None:
         (sx, sy, sz), wav = source
         c.add('static const float _src[%d] = {%s};' % (len(wav), ', '.join(repr(float(w)) + 'f' for w in wav)))
+    nrec = len(receivers) if receivers is not None else 0
+    if nrec:
+        c.add('static float _traces[%d][4][%d];' % (grid.ntsteps.value, nrec))
     c.add('extern "C" int opesci_execute(OpesciGrid *grid, OpesciProfiling *profiling){')
     c.add(define_constants(grid))
     c.add(declare_fields(grid))
@@ -322,6 +329,15 @@ def generate(grid, legacy=False, dump_prefix=None, source=None, timer=True):
                  '%s[_t1][%d][%d][%d] -= _src[_ti]/3;' % (names[3], sx, sy, sz),
                  '%s[_t1][%d][%d][%d] -= _src[_ti]/3;' % (names[4], sx, sy, sz),
                  '%s[_t1][%d][%d][%d] -= _src[_ti]/3;' % (names[5], sx, sy, sz), '}', '}']
+    if nrec:
+        loop += ['#pragma omp single', '{']
+        for r, (x, y, z) in enumerate(receivers):
+            at = '[_t1][%d][%d][%d]' % (x, y, z)
+            loop += ['_traces[_ti][0][%d] = %s%s;' % (r, names[0], at),
+                     '_traces[_ti][1][%d] = %s%s;' % (r, names[1], at),
+                     '_traces[_ti][2][%d] = %s%s;' % (r, names[2], at),
+                     '_traces[_ti][3][%d] = (%s%s + %s%s + %s%s)/3;' % (r, names[3], at, names[4], at, names[5], at)]
+        loop += ['}']
     c.add(['for(int _ti=0;_ti<ntsteps;_ti++){'] + loop + ['}'])
     c.add('#pragma omp barrier')
     c.add('#pragma omp master')
@@ -337,6 +353,9 @@ def generate(grid, legacy=False, dump_prefix=None, source=None, timer=True):
         for nm in names:
             c.add('{ FILE* fp = fopen("%s%s.raw", "wb"); fwrite(&%s[%d][0][0][0], sizeof(%s), %d, fp); fclose(fp); }'
                   % (dump_prefix, nm, nm, lvl, grid.real_t, n))
+    if nrec and dump_prefix:
+        c.add('{ FILE* fp = fopen("%straces.raw", "wb"); fwrite(_traces, sizeof(float), %d, fp); fclose(fp); }'
+              % (dump_prefix, grid.ntsteps.value * 4 * nrec))
     c.add('return 0;')
     c.add('}')
     # convergence

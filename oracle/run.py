@@ -40,13 +40,13 @@ def compile_program(src, workdir, vectorize=False):
     return exe
 
 
-def run(grid, workdir, legacy=False, source=None, threads=None, vectorize=False, dump=True):
+def run(grid, workdir, legacy=False, source=None, threads=None, vectorize=False, dump=True, receivers=None):
     """Emit, compile and run the oracle program for ``grid``.  Returns a dict
     with 'l2' (float-accumulated, as the reference prints), 'l2_fp64',
     'loop_seconds', 'threads' and 'fields' (final level, reference layout)."""
     workdir = os.path.abspath(workdir)
     prefix = os.path.join(workdir, "dump_") if dump else None
-    src = cpp_emitter.generate(grid, legacy=legacy, dump_prefix=prefix, source=source)
+    src = cpp_emitter.generate(grid, legacy=legacy, dump_prefix=prefix, source=source, receivers=receivers)
     exe = compile_program(src, workdir, vectorize=vectorize)
     env = dict(os.environ)
     nthreads = threads or os.cpu_count() or 1
@@ -67,4 +67,7 @@ def run(grid, workdir, legacy=False, source=None, threads=None, vectorize=False,
         dims = tuple(d.value for d in grid.dim)
         real = np.float64 if grid.double else np.float32
         out['fields'] = {f: np.fromfile(prefix + f + '.raw', dtype=real).reshape(dims) for f in FIELDS}
+        if receivers:
+            out['traces'] = np.fromfile(prefix + 'traces.raw', dtype=np.float32).reshape(
+                grid.ntsteps.value, 4, len(receivers))
     return out

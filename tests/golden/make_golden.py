@@ -13,7 +13,15 @@ Writes
   notebook_outputs.json   the text outputs of the known-answer cells of the
                           reference notebooks tests/eigenwave3d.ipynb and
                           tests/eigenwave3d-read.ipynb, verbatim.
+  resample.json           inputs and outputs of the reference's own trace
+                          resampling opesci_resample_timeseries
+                          (src/opesciHandy.cpp:125-195), compiled from where
+                          it lies by oracle/Makefile into
+                          oracle/_ref/libopescihandy.so, on seeded series
+                          (up- and downsampling, odd and even lengths).
 Nothing at test time reads the reference; tests read only these files.
+
+    python tests/golden/make_golden.py --only resample    # just resample.json
 """
 import argparse
 import json
@@ -39,14 +47,43 @@ def notebook_cells(path, cells):
     return out
 
 
+def resample_fixtures():
+    """Run the reference's opesci_resample_timeseries on seeded series."""
+    import ctypes
+    import numpy as np
+    lib = ctypes.CDLL(os.path.join(ROOT, 'oracle', '_ref', 'libopescihandy.so'))
+    fp = ctypes.POINTER(ctypes.c_float)
+    lib.ref_resample_timeseries.argtypes = [fp, ctypes.c_int, ctypes.c_float, ctypes.c_double, fp, ctypes.c_int]
+    rng = np.random.default_rng(20150101)
+    cases = []
+    for n, dt, sdt, kind in ((100, 1e-3, 2e-3, 'ricker'), (101, 2e-3, 1e-3, 'ricker'), (64, 0.7e-3, 1e-3, 'noise'),
+                             (257, 1e-3, 0.9e-3, 'ricker'), (300, 4e-4, 1e-3, 'noise'), (50, 1e-3, 1e-3, 'noise')):
+        t = np.arange(n) * sdt
+        if kind == 'ricker':
+            a = (np.pi * 20.0 * (t - 1.0 / 20.0)) ** 2
+            src = ((1 - 2 * a) * np.exp(-a)).astype(np.float32)
+        else:
+            src = rng.standard_normal(n).astype(np.float32)
+        out = np.zeros(4 * n + 16, dtype=np.float32)
+        m = lib.ref_resample_timeseries(src.ctypes.data_as(fp), n, dt, sdt, out.ctypes.data_as(fp), len(out))
+        cases.append({'dt': dt, 'sdt': sdt, 'src': [float(x) for x in src],
+                      'resampled': [float(x) for x in out[:m]]})
+    json.dump({'function': 'opesci_resample_timeseries (src/opesciHandy.cpp:125-195)', 'cases': cases},
+              open(os.path.join(HERE, 'resample.json'), 'w'))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--reference', default='/root/reference')
     ap.add_argument('--threads', type=int, default=os.cpu_count())
+    ap.add_argument('--only', choices=['resample'], default=None)
     args = ap.parse_args()
 
     subprocess.check_call(['make', '-C', os.path.join(ROOT, 'oracle'),
                            'REFERENCE=' + args.reference])
+    resample_fixtures()
+    if args.only == 'resample':
+        return
     env = dict(os.environ, OMP_NUM_THREADS=str(args.threads))
     out = subprocess.check_output([os.path.join(ROOT, 'oracle', '_ref', 'test3d')],
                                   env=env, text=True)
