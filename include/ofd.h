@@ -113,6 +113,14 @@ int ofd_set_receivers(ofd_handle *h, int nrec, const int *ijk, int nt_cap);
 /* copy the whole trace buffer (nt_cap * 4 * nrec floats) to host memory */
 int ofd_get_traces(ofd_handle *h, float *host);
 
+/* SEG-Y earth model decoding (the reference's opesci_read_model_segy,
+ * src/opesciIO.cpp:419-612, format code 1): file is the whole SEG-Y image in
+ * host memory, (nx, ny, nz) traces per record, records and samples per trace
+ * from its header, swap_endian whether the header was read byte-swapped.
+ * The IBM-float samples are decoded on the device into out[nz][ny][nx] (host
+ * memory, x fastest, the reference's array order).  No handle needed. */
+int ofd_segy_decode_ibm(const void *file, long file_size, int nx, int ny, int nz, int swap_endian, float *out);
+
 /* Ghost cells of one level as the reference's initialise_bc does for the
  * initial level (staggeredgrid.py:866-879): stress mirrors, then velocity
  * ghosts. */

@@ -249,6 +249,11 @@ bool build_maps(ofd_handle *h) {
 
 }  // namespace
 
+namespace ofd {
+// ofd_segy.cu
+cudaError_t segy_decode(const void *file, long file_size, int nx, int ny, int nz, int swap, float *out);
+}  // namespace ofd
+
 extern "C" {
 
 const char *ofd_last_error(void) { return g_last_error.c_str(); }
@@ -781,6 +786,18 @@ int ofd_group_create(ofd_handle *const *hs, int n, int chunk_planes, ofd_group *
     return fail(OFD_ECUDA, "group setup failed: %s", cudaGetErrorString(e));
   }
   *out = g;
+  return OFD_OK;
+}
+
+int ofd_segy_decode_ibm(const void *file, long file_size, int nx, int ny, int nz, int swap_endian, float *out) {
+  if (!file || !out) return fail(OFD_EINVAL, "null argument");
+  if (nx <= 0 || ny <= 0 || nz <= 0) return fail(OFD_EINVAL, "bad model dimensions %d x %d x %d", nx, ny, nz);
+  const long need = 3600 + (long)nx * ny * (240 + 4L * nz);
+  if (file_size < need)
+    return fail(OFD_EINVAL, "SEG-Y image of %ld bytes is shorter than its %d x %d traces (%ld bytes)", file_size, nx,
+                ny, need);
+  const cudaError_t e = ofd::segy_decode(file, file_size, nx, ny, nz, swap_endian, out);
+  if (e != cudaSuccess) return fail(OFD_ECUDA, "SEG-Y decode: %s", cudaGetErrorString(e));
   return OFD_OK;
 }
 

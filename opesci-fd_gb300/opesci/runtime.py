@@ -93,6 +93,8 @@ def load_library():
         'ofd_group_create': [P(h), ctypes.c_int, ctypes.c_int, P(h)],
         'ofd_group_step': [h, ctypes.c_int],
         'ofd_group_eligible': [h],
+        'ofd_segy_decode_ibm': [ctypes.c_void_p, ctypes.c_long, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                ctypes.c_int, fptr],
         'ofd_group_query': [h],
         'ofd_group_sync': [h],
         'ofd_group_destroy': [h],

@@ -18,10 +18,17 @@ Writes
                           (src/opesciHandy.cpp:125-195), compiled from where
                           it lies by oracle/Makefile into
                           oracle/_ref/libopescihandy.so, on seeded series
-                          (up- and downsampling, odd and even lengths).
+                          (up- and downsampling, odd and even lengths);
+  model_be.segy, model_le.segy, segy.json
+                          small format-1 SEG-Y models (big- and little-endian,
+                          with planted IBM words: negative zero, underflow,
+                          overflow, extremes) and what the reference's own
+                          opesci_read_model_segy (src/opesciIO.cpp:419-612),
+                          compiled into the same library, reads from them.
 Nothing at test time reads the reference; tests read only these files.
 
     python tests/golden/make_golden.py --only resample    # just resample.json
+    python tests/golden/make_golden.py --only segy        # just the SEG-Y fixtures
 """
 import argparse
 import json
@@ -72,17 +79,62 @@ def resample_fixtures():
               open(os.path.join(HERE, 'resample.json'), 'w'))
 
 
+SEGY_RAW_WORDS = [0x80000000, 0x00000001, 0x7FFFFFFF, 0xFFFFFFFF, 0xC1100000, 0x41100000, 0x00FFFFFF,
+                  0x21000001, 0x60FFFFFF, 0x3F7FFFFF]
+
+
+def segy_fixtures():
+    """Small format-1 SEG-Y models (big- and little-endian) read by the
+    reference's opesci_read_model_segy; the files are kept as fixtures."""
+    import ctypes
+    import sys
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, 'opesci-fd_gb300'))
+    from opesci import segy
+    lib = ctypes.CDLL(os.path.join(ROOT, 'oracle', '_ref', 'libopescihandy.so'))
+    fp = ctypes.POINTER(ctypes.c_float)
+    lib.ref_read_model_segy.argtypes = [ctypes.c_char_p, fp, ctypes.c_long, ctypes.POINTER(ctypes.c_int), fp]
+    rng = np.random.default_rng(1998)
+    nz, ny, nx = 11, 5, 7
+    model = (1500.0 + 3000.0 * rng.random((nz, ny, nx))).astype(np.float32)
+    model[0, 0, :4] = [0.0, -2.5, 1e-30, 3.0e30]
+    out = {}
+    for name, big in (('model_be.segy', True), ('model_le.segy', False)):
+        path = os.path.join(HERE, name)
+        segy.write_model_segy(path, model, dx=12.5, dz=10.0, big_endian=big)
+        # plant raw IBM words (negative zero, underflow, overflow, extremes)
+        data = bytearray(open(path, 'rb').read())
+        tracesize = 240 + 4 * nz
+        for k, w in enumerate(SEGY_RAW_WORDS):
+            tr, iz = 3 + k // nz, k % nz
+            off = 3600 + tr * tracesize + 240 + 4 * iz
+            data[off:off + 4] = w.to_bytes(4, 'big' if big else 'little')
+        open(path, 'wb').write(bytes(data))
+        buf = np.zeros(nx * ny * nz, dtype=np.float32)
+        dims = (ctypes.c_int * 3)()
+        sp = np.zeros(3, dtype=np.float32)
+        m = lib.ref_read_model_segy(path.encode(), buf.ctypes.data_as(fp), len(buf), dims, sp.ctypes.data_as(fp))
+        assert m == len(buf), m
+        out[name] = {'dims': list(dims), 'spacing': [float(x) for x in sp],
+                     'values_hex': [format(int(v), '08x') for v in buf.view(np.uint32)]}
+    json.dump({'function': 'opesci_read_model_segy (src/opesciIO.cpp:419-612)', 'files': out},
+              open(os.path.join(HERE, 'segy.json'), 'w'))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--reference', default='/root/reference')
     ap.add_argument('--threads', type=int, default=os.cpu_count())
-    ap.add_argument('--only', choices=['resample'], default=None)
+    ap.add_argument('--only', choices=['resample', 'segy'], default=None)
     args = ap.parse_args()
 
     subprocess.check_call(['make', '-C', os.path.join(ROOT, 'oracle'),
                            'REFERENCE=' + args.reference])
-    resample_fixtures()
-    if args.only == 'resample':
+    if args.only in (None, 'resample'):
+        resample_fixtures()
+    if args.only in (None, 'segy'):
+        segy_fixtures()
+    if args.only is not None:
         return
     env = dict(os.environ, OMP_NUM_THREADS=str(args.threads))
     out = subprocess.check_output([os.path.join(ROOT, 'oracle', '_ref', 'test3d')],
