@@ -32,9 +32,11 @@ METRIC = 'elastic GLUP/s (grid-point updates of all 9 fields per second), 512^3 
 UNIT = 'GLUP/s'
 # algorithmic bytes per grid point of each sweep (FP32 fields, FP32 media):
 # stress reads U V W + 6 stresses + lambda mu mu12 mu13 mu23, writes 6 stresses
-# velocity reads U V W + 6 stresses + beta1..3, writes U V W
+# (80 B); velocity reads U V W + 6 stresses + beta (beta1..3 are formed from
+# beta and its neighbours on the fly), writes U V W (52 B).  The reference's
+# formulation, with beta1..3 as three arrays, needs 140 B per point.
 STRESS_BYTES_PER_LUP = 4 * (9 + 5 + 6)
-VELOCITY_BYTES_PER_LUP = 4 * (9 + 3 + 3)
+VELOCITY_BYTES_PER_LUP = 4 * (9 + 1 + 3)
 STEP_BYTES_PER_LUP = STRESS_BYTES_PER_LUP + VELOCITY_BYTES_PER_LUP
 
 
@@ -230,7 +232,7 @@ def main():
     vel_ms = cls_ms[2] / args.steps
     esz = {'f32': 4, 'f16': 2, 'bf16': 2, 'f64': 8}.get(args.storage, 4)
     sb = (9 + 6) * esz + 5 * 4
-    vb = (9 + 3) * esz + 3 * 4
+    vb = (9 + 3) * esz + 4
     stress_bytes = float(n) ** 3 * sb
     achieved = stress_bytes / (stress_ms / 1e3) / 1e9
     tr = profiled_traffic('stress_sweep_so%d_%s' % (so, args.storage))

@@ -20,7 +20,10 @@
 namespace ofd {
 
 enum { F_U = 0, F_V, F_W, F_TXX, F_TYY, F_TZZ, F_TXY, F_TYZ, F_TXZ, NF };
-enum { M_LAM = 0, M_MU, M_MU12, M_MU13, M_MU23, M_B1, M_B2, M_B3, NM };
+// media arrays: lambda, mu, the effective shear moduli, the averaged
+// buoyancies and the buoyancy beta = 1/rho itself (from which the tiled
+// velocity sweep forms beta1..3 on the fly)
+enum { M_LAM = 0, M_MU, M_MU12, M_MU13, M_MU23, M_B1, M_B2, M_B3, M_BETA, NM };
 
 // Storage traits: S is the stored type, C the arithmetic type.  16-bit
 // storage keeps value*scale (scale a power of two, so scaling is exact).

@@ -52,7 +52,7 @@ __global__ void media_base_kernel(const float *rho, const float *vp, const float
 
 __global__ void media_avg_kernel(const float *beta, const float *lam, const float *mu, const double *im, Geom g,
                                  float *o_lam, float *o_mu, float *o_mu12, float *o_mu13,
-                                 float *o_mu23, float *o_b1, float *o_b2, float *o_b3) {
+                                 float *o_mu23, float *o_b1, float *o_b2, float *o_b3, float *o_beta) {
   const long n = (long)g.n1 * g.n2 * g.n3;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
     const int z = (int)(i % g.n3);
@@ -65,6 +65,7 @@ __global__ void media_avg_kernel(const float *beta, const float *lam, const floa
     o_lam[o] = lam[i];
     o_mu[o] = mu[i];
     const float b0 = beta[i];
+    o_beta[o] = b0;
     o_b1[o] = (b0 + beta[D(x1, y, z)]) * 0.5f;
     o_b2[o] = (b0 + beta[D(x, y1, z)]) * 0.5f;
     o_b3[o] = (b0 + beta[D(x, y, z1)]) * 0.5f;
@@ -238,6 +239,11 @@ bool build_maps(ofd_handle *h) {
     }
   for (int i = 0; i < NM && ok; ++i)
     ok = encode(&mp->media[i], (void *)(h->s.media[i] - h->s.z0), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, g, pw, ph);
+  if (ok) {
+    int bw, bh;
+    beta_box(h->s.R, &bw, &bh);
+    ok = encode(&mp->beta, (void *)(h->s.media[M_BETA] - h->s.z0), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, g, bw, bh);
+  }
   if (!ok) {
     delete mp;
     return false;
@@ -411,7 +417,7 @@ int ofd_set_coefficients(ofd_handle *h, int het, const float *ks, int nks, const
 int ofd_set_media_const(ofd_handle *h, float beta, float lambda, float mu) {
   if (!h) return fail(OFD_EINVAL, "null handle");
   const long n = h->media_elems;
-  const float vals[NM] = {lambda, mu, mu, mu, mu, beta, beta, beta};
+  const float vals[NM] = {lambda, mu, mu, mu, mu, beta, beta, beta, beta};
   for (int i = 0; i < NM; ++i)
     fill_kernel<<<1216, 256, 0, h->stream>>>(h->s.media[i] - h->s.z0, n, vals[i]);
   OFD_CUDA(cudaGetLastError());
@@ -435,7 +441,7 @@ int ofd_set_media(ofd_handle *h, const float *rho, const float *vp, const float 
   media_avg_kernel<<<1216, 256, 0, h->stream>>>(tmp + 3 * n, tmp + 4 * n, tmp + 5 * n, inv_mu, g, h->s.media[M_LAM],
                                                 h->s.media[M_MU], h->s.media[M_MU12], h->s.media[M_MU13],
                                                 h->s.media[M_MU23], h->s.media[M_B1], h->s.media[M_B2],
-                                                h->s.media[M_B3]);
+                                                h->s.media[M_B3], h->s.media[M_BETA]);
   OFD_CUDA(cudaGetLastError());
   OFD_CUDA(cudaFreeAsync(tmp, h->stream));
   OFD_CUDA(cudaStreamSynchronize(h->stream));

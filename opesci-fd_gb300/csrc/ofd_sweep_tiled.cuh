@@ -44,7 +44,8 @@ template <typename S> struct ZHalo { static constexpr int v = (int)(16 / sizeof(
 struct TmaMaps {
   CUtensorMap halo[9][2];
   CUtensorMap point[9][2];
-  CUtensorMap media[8];
+  CUtensorMap media[NM];
+  CUtensorMap beta;      // (TZ + 4) x (TY + 1) boxes of beta: the point, y + 1 and z + 1
   int ok;
 };
 
@@ -57,6 +58,11 @@ struct TiledCtx {
 };
 
 // Box extents the runtime encodes into the descriptors.
+inline void beta_box(int R, int *bw, int *bh) {
+  *bw = TZ + 4;
+  *bh = tile_rows(R) + 1;
+}
+
 inline void tiled_boxes(int R, int esize, int *hw, int *hh, int *pw, int *ph) {
   const int zh = (16 / esize) >= 4 ? 16 / esize : 4;
   *hw = TZ + 2 * zh;
@@ -69,6 +75,7 @@ struct TiledParams {
   CUtensorMap hmap[6];     // halo boxes: x-window arrays, then plane-halo arrays
   CUtensorMap pmap[6];     // point boxes of field arrays
   CUtensorMap mmap[5];     // point boxes of media arrays
+  CUtensorMap bmap;        // beta boxes (heterogeneous velocity sweep)
   int *err;                // error word (bounded waits)
   int zcoord0;             // TMA x coordinate of z = m (z0 + m)
   int chunk;               // planes per CTA along x
@@ -158,7 +165,13 @@ struct TiledCfg {
   static constexpr int NXF = 3;                            // x-window arrays
   static constexpr int NH0 = STRESS ? 0 : 3;               // plane-halo arrays
   static constexpr int NPF = STRESS ? 6 : 3;               // point field arrays
-  static constexpr int NMF = HET ? (STRESS ? 5 : 3) : 0;   // point media arrays
+  // point media arrays: lambda mu mu12 mu13 mu23 (stress).  The velocity
+  // sweep reads beta instead of beta1..3, as one box per x-window plane
+  // covering the point, y + 1 and z + 1 (z extent rounded to 16 bytes), and
+  // averages on the fly exactly as the media preprocessing does.
+  static constexpr int NMF = (HET && STRESS) ? 5 : 0;
+  static constexpr int NBX = (HET && !STRESS) ? 1 : 0;    // beta box per x-window plane
+  static constexpr int BW = TZ + 4, BH = TY + 1;          // beta box extent (floats)
   static constexpr int PF = 1;                             // planes prefetched ahead
   static constexpr int NSH = 2 * R + 1 + PF;               // x-window ring depth
   static constexpr int NSC = 1 + PF;                       // plane ring depth
@@ -170,13 +183,15 @@ struct TiledCfg {
   static constexpr int MSLOT = round128(MBOX);
   // one x-window ring stage holds NXF halo boxes; one plane ring stage holds
   // NH0 halo boxes, NPF point boxes and NMF media boxes
-  static constexpr int XSTAGE = NXF * HSLOT;
+  static constexpr int BBOX = BW * BH * 4;
+  static constexpr int BSLOT = round128(BBOX);
+  static constexpr int XSTAGE = NXF * HSLOT + NBX * BSLOT;
   static constexpr int CSTAGE = NH0 * HSLOT + NPF * PSLOT + NMF * MSLOT;
   static constexpr int XRING = NSH * XSTAGE;
   static constexpr int CRING = NSC * CSTAGE;
   static constexpr int BARS = 2 * (NSH + NSC) * 8;        // full and empty barrier per slot
   static constexpr int SMEM = XRING + CRING + round128(BARS) + 128;  // +128: base alignment
-  static constexpr unsigned XBYTES = NXF * HBOX;
+  static constexpr unsigned XBYTES = NXF * HBOX + NBX * BBOX;
   static constexpr unsigned CBYTES = NH0 * HBOX + NPF * PBOX + NMF * MBOX;
   // role and index of a field id
   __host__ __device__ static constexpr int role(int f) {   // 0 X, 1 H, 2 P
@@ -206,7 +221,7 @@ struct TiledAcc {
   const unsigned char *xs[2 * R + 1];
   const unsigned char *cs;
   const float *inv;
-  int hpos, ppos;
+  int hpos, ppos, bpos;
   __device__ __forceinline__ C operator()(int f, int dx, int dy, int dz) const {
     const int off = dy * G::HW + dz;
     if (G::role(f) == 0) {
@@ -221,6 +236,16 @@ struct TiledAcc {
     return (C)Storage<S>::load(b[ppos], inv[f]);
   }
   __device__ __forceinline__ C m(int i) const {
+    if constexpr (G::NBX != 0) {
+      // beta1..3 = (beta + beta at x+1 / y+1 / z+1) * 0.5f, as media_avg_kernel
+      const float *b = (const float *)(xs[R] + G::NXF * G::HSLOT);
+      const float b0 = b[bpos];
+      float b1;
+      if (i == M_B1) b1 = ((const float *)(xs[R + 1] + G::NXF * G::HSLOT))[bpos];
+      else if (i == M_B2) b1 = b[bpos + G::BW];
+      else b1 = b[bpos + 1];
+      return (C)((b0 + b1) * 0.5f);
+    }
     const float *b = (const float *)(cs + G::moff(G::midx(i)));
     return (C)b[ppos];
   }
@@ -278,6 +303,7 @@ __device__ __forceinline__ void sweep_tile(const SweepArgs<S> &a, const TiledPar
     unsigned char *st = xring + slot * G::XSTAGE;
 #pragma unroll
     for (int i = 0; i < G::NXF; ++i) tma_load_3d(st + i * G::HSLOT, &p.hmap[i], bar, zc - G::ZH, y0 - R, plane);
+    if constexpr (G::NBX != 0) tma_load_3d(st + G::NXF * G::HSLOT, &p.bmap, bar, zc, y0, plane);
   };
   auto issue_c = [&](int plane) {
     const int slot = (plane - xb) % G::NSC;
@@ -368,6 +394,7 @@ __device__ __forceinline__ void sweep_tile(const SweepArgs<S> &a, const TiledPar
         const int z = z0 + zl;
         A.hpos = (yl + R) * G::HW + zl + G::ZH;
         A.ppos = yl * TZ + zl;
+        A.bpos = yl * G::BW + zl;
         const long o = (long)x * g.plane + (long)y * g.P + z;
         const bool inside = (z < g.n3 - g.m) && (y < g.n2 - g.m);
         if (STRESS) {
@@ -467,6 +494,7 @@ sweep_tiled_group(const GroupSweep<S> *__restrict__ tab, int n) {
 #pragma unroll 1
     for (int i = 0; i < G::NMF; ++i)
       asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(&e.p.mmap[i]) : "memory");
+    if (G::NBX) asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(&e.p.bmap) : "memory");
   }
   const int local = (int)blockIdx.x - e.cta_begin;
   if constexpr (KD) {
@@ -513,7 +541,7 @@ void tiled_params(const SweepArgs<S> &a, const TiledCtx &ctx, int t0, int chunk_
     const int order[6] = {F_TXX, F_TXY, F_TXZ, F_TYY, F_TYZ, F_TZZ};
     for (int i = 0; i < 6; ++i) p.hmap[i] = mp->halo[order[i]][t1];
     for (int i = 0; i < 3; ++i) p.pmap[i] = mp->point[F_U + i][t0];
-    for (int i = 0; i < 3; ++i) p.mmap[i] = mp->media[M_B1 + i];
+    if (G::NBX) p.bmap = mp->beta;
   }
   p.err = ctx.err;
   p.zcoord0 = ctx.z0 + g.m;
