@@ -194,8 +194,7 @@ def main():
         import torch.distributed as dist
         torch.cuda.set_device(local)
         dist.init_process_group('nccl')
-    else:
-        runtime.load_library()
+    runtime.set_device(local)   # libofd carries its own CUDA runtime
 
     n, so = args.size, args.space_order
     g, media, src, wav = build_problem(n, so, args.warmup + args.steps)
@@ -218,14 +217,11 @@ def main():
     if dist is not None:
         dist.barrier()
     clocks = sampler.stop()
-    ms = total_ms
-    if dist is not None:
-        import torch
-        t = torch.tensor([ms], dtype=torch.float64, device='cuda')
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    from opesci import replicas
     lups_rank = float(n) ** 3 * args.steps
-    value = lups_rank * world / (ms / 1e3) / 1e9
+    rate, secs = replicas.aggregate_rate(lups_rank, total_ms / 1e3, dist, device='cuda')
+    ms = secs * 1e3
+    value = rate / 1e9
 
     peak, peak_src = measured_peak()
     stress_ms = cls_ms[0] / args.steps

@@ -61,6 +61,13 @@ typedef struct ofd_config {
 
 typedef struct ofd_handle ofd_handle;
 
+/* Device for handles created afterwards by the calling thread (no
+ * counterpart in the reference, which runs on the host).  The library
+ * carries its own CUDA runtime, so a device chosen through another runtime
+ * (a framework's) does not apply to it; one process per GPU calls this with
+ * its local rank. */
+int ofd_set_device(int device);
+
 /* Lifecycle.  ofd_create allocates two time levels of the nine fields and the
  * eight effective-media arrays on the current device, all zero. */
 int ofd_create(const ofd_config *cfg, ofd_handle **out);

@@ -795,6 +795,16 @@ int ofd_group_create(ofd_handle *const *hs, int n, int chunk_planes, ofd_group *
   return OFD_OK;
 }
 
+int ofd_set_device(int device) {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess) return fail(OFD_ECUDA, "cudaGetDeviceCount: %s", cudaGetErrorString(e));
+  if (device < 0 || device >= n) return fail(OFD_EINVAL, "device %d outside 0..%d", device, n - 1);
+  e = cudaSetDevice(device);
+  if (e != cudaSuccess) return fail(OFD_ECUDA, "cudaSetDevice(%d): %s", device, cudaGetErrorString(e));
+  return OFD_OK;
+}
+
 int ofd_segy_decode_ibm(const void *file, long file_size, int nx, int ny, int nz, int swap_endian, float *out) {
   if (!file || !out) return fail(OFD_EINVAL, "null argument");
   if (nx <= 0 || ny <= 0 || nz <= 0) return fail(OFD_EINVAL, "bad model dimensions %d x %d x %d", nx, ny, nz);

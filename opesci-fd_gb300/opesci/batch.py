@@ -234,7 +234,11 @@ def main():
     ap.add_argument('--chunk-planes', type=int, default=0, help='x planes per sweep CTA in groups (0: heuristic)')
     args = ap.parse_args()
     os.environ.setdefault('CUDA_DEVICE_MAX_CONNECTIONS', '32')
-    shots = make_shots(args.shots, args.seed)
+    # under torchrun: one replica per GPU, shots split round robin
+    from . import replicas
+    rank, world, local = replicas.rank_env()
+    runtime.set_device(local)
+    shots = replicas.shard(make_shots(args.shots, args.seed), rank, world)
     lups = sum(s.lups for s in shots)
     # synthesise every shot's inputs once, outside both timings
     t0 = time.perf_counter()
@@ -256,6 +260,7 @@ def main():
         to, _ = run_one_by_one(shots, built=built)
         res.update({'one_by_one_s': to, 'one_by_one_glups': lups / to / 1e9, 'speedup': to / tg,
                     'speedup_streams': to / tb})
+    res.update({'rank': rank, 'world': world})
     print(json.dumps(res))
 
 

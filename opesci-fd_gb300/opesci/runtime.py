@@ -92,6 +92,7 @@ def load_library():
         'ofd_field_view_get': [h, ctypes.c_int, ctypes.c_int, P(ofd_field_view)],
         'ofd_group_create': [P(h), ctypes.c_int, ctypes.c_int, P(h)],
         'ofd_group_step': [h, ctypes.c_int],
+        'ofd_set_device': [ctypes.c_int],
         'ofd_group_eligible': [h],
         'ofd_segy_decode_ibm': [ctypes.c_void_p, ctypes.c_long, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                 ctypes.c_int, fptr],
@@ -109,6 +110,13 @@ def load_library():
     lib.ofd_stream.restype = ctypes.c_void_p
     _lib = lib
     return lib
+
+
+def set_device(index):
+    """Device of the simulations this thread creates next (one process per
+    GPU passes its local rank)."""
+    lib = load_library()
+    _check(lib.ofd_set_device(int(index)), 'ofd_set_device')
 
 
 def _check(rc, what):
