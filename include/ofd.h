@@ -190,6 +190,11 @@ int ofd_group_query(ofd_group *g);
 int ofd_group_sync(ofd_group *g);
 int ofd_group_destroy(ofd_group *g);
 
+/* ofd_step bracketed by CUDA events on the handle's stream (no events
+ * between kernels); waits; ms = elapsed time, launches (may be NULL) =
+ * kernels run. */
+int ofd_step_timed(ofd_handle *h, int nsteps, double *ms, long *launches);
+
 /* completed steps; the newest level is steps % 2 */
 int ofd_get_step(ofd_handle *h, long *steps);
 int ofd_set_step(ofd_handle *h, long steps);

@@ -734,6 +734,33 @@ int ofd_step_graph(ofd_handle *h, int nsteps) {
   return OFD_OK;
 }
 
+int ofd_step_timed(ofd_handle *h, int nsteps, double *ms, long *launches) {
+  if (!h || !ms) return fail(OFD_EINVAL, "null argument");
+  if (nsteps <= 0) return fail(OFD_EINVAL, "nsteps must be > 0");
+  if (h->s.nks == 0) return fail(OFD_ESTATE, "ofd_set_coefficients has not been called");
+  if (h->s.persistent) return fail(OFD_ESTATE, "timed stepping runs the launch path; persistent stepping is on");
+  cudaEvent_t a = nullptr, b = nullptr;
+  cudaError_t e = cudaEventCreate(&a);
+  if (e == cudaSuccess) e = cudaEventCreate(&b);
+  if (e == cudaSuccess) e = cudaEventRecord(a, h->stream);
+  int rc = OFD_OK;
+  if (e == cudaSuccess) {
+    rc = ofd_step(h, nsteps);
+    if (rc == OFD_OK) e = cudaEventRecord(b, h->stream);
+  }
+  float f = 0.f;
+  if (e == cudaSuccess && rc == OFD_OK) e = cudaEventSynchronize(b);
+  if (e == cudaSuccess && rc == OFD_OK) e = cudaEventElapsedTime(&f, a, b);
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  if (rc != OFD_OK) return rc;
+  if (e != cudaSuccess) return fail(OFD_ECUDA, "event timing: %s", cudaGetErrorString(e));
+  *ms = f;
+  if (launches) *launches = (long)nsteps * h->be->launches_per_step(h->s);
+  return check_err_word(h);
+}
+
+
 // ------------------------------------------------------------- groups
 
 struct ofd_group {

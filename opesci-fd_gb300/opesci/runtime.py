@@ -81,6 +81,7 @@ def load_library():
         'ofd_step': [h, ctypes.c_int],
         'ofd_step_graph': [h, ctypes.c_int],
         'ofd_set_persistent': [h, ctypes.c_int],
+        'ofd_step_timed': [h, ctypes.c_int, P(ctypes.c_double), P(ctypes.c_long)],
         'ofd_set_tuning': [h, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int],
         'ofd_step_profiled': [h, ctypes.c_int, P(ctypes.c_double), P(ctypes.c_double), P(ctypes.c_long)],
         'ofd_sync': [h],
@@ -275,6 +276,14 @@ class Simulation(object):
     def step_graph(self, n):
         """Advance n steps by replaying a captured two-step CUDA graph."""
         _check(self.lib.ofd_step_graph(self.h, int(n)), 'ofd_step_graph')
+
+    def step_timed(self, n):
+        """n steps on the launch path, timed with CUDA events on the
+        handle's stream only around all of them: (ms, kernel launches)."""
+        ms = ctypes.c_double()
+        nl = ctypes.c_long()
+        _check(self.lib.ofd_step_timed(self.h, int(n), ctypes.byref(ms), ctypes.byref(nl)), 'ofd_step_timed')
+        return ms.value, nl.value
 
     def set_persistent(self, enable=True):
         """Run time steps in cooperative launches of up to 1024 steps."""

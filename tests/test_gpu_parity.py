@@ -158,6 +158,8 @@ def run_random_state(so, n, faces, storage, mode, steps=6):
     if mode == 'persistent':
         sim.set_persistent(1)
         sim.step_graph(steps)
+    elif mode == 'graph':
+        sim.step_graph(steps)
     else:
         sim.step(steps)
     sim.sync()
@@ -169,18 +171,21 @@ def run_random_state(so, n, faces, storage, mode, steps=6):
 @pytest.mark.parametrize('so,n,faces,storage', [
     (4, 72, 'levander', 'f32'), (4, 70, 'mixed', 'f32'), (4, 66, 'zfree', 'f32'), (4, 72, 'levander', 'f16'),
     (8, 68, 'robertsson', 'f32'), (6, 67, 'mixed', 'f32'), (2, 70, 'robertsson', 'f32'),
-    (8, 66, 'robertsson', 'bf16')])
+    (8, 66, 'robertsson', 'bf16'),
+    # four z tiles
+    (4, 200, 'levander', 'f32'), (8, 196, 'mixed', 'f32'), (4, 193, 'zfree', 'f16')])
 def test_boundary_paths_identical_across_kernels(so, n, faces, storage):
-    """Tiled sweeps (z-face stress ghosts of inner columns fused into the
-    stress sweep), plain sweeps (every ghost phase in its own launch) and
-    persistent stepping agree bit for bit with every boundary active."""
+    """Tiled sweeps (launches and graphs), plain sweeps and persistent
+    stepping agree bit for bit with every boundary active."""
     a = run_random_state(so, n, FACE_MIXES[faces], storage, 'tiled')
     b = run_random_state(so, n, FACE_MIXES[faces], storage, 'plain')
     c = run_random_state(so, n, FACE_MIXES[faces], storage, 'persistent')
+    e = run_random_state(so, n, FACE_MIXES[faces], storage, 'graph')
     for f in runtime.FIELDS:
         assert np.isfinite(a[f]).all(), f
         assert np.array_equal(a[f], b[f]), ('tiled/plain', f)
         assert np.array_equal(b[f], c[f]), ('plain/persistent', f)
+        assert np.array_equal(a[f], e[f]), ('steps/graph', f)
 
 
 def test_tiled_constant_media_identical():
