@@ -109,6 +109,11 @@ def load_library():
     lib.ofd_last_error.restype = ctypes.c_char_p
     lib.ofd_stream.argtypes = [h]
     lib.ofd_stream.restype = ctypes.c_void_p
+    lib.ofd_sumsq_field_noalloc.argtypes = [ctypes.c_void_p, P(ctypes.c_int), ctypes.c_int, ctypes.c_void_p,
+                                            ctypes.c_void_p]
+    lib.ofd_sumsq_field_noalloc.restype = ctypes.c_int
+    lib.ofd_noalloc_last_error.argtypes = []
+    lib.ofd_noalloc_last_error.restype = ctypes.c_char_p
     _lib = lib
     return lib
 

@@ -51,3 +51,12 @@ def test_footprint_and_validation_without_gpu(lib):
     with pytest.raises(runtime.OFDError, match='too small'):
         runtime.Simulation.footprint(small)
     assert 'too small' in lib.ofd_last_error().decode()
+
+
+def test_python_binding_covers_every_entry_point(lib):
+    """opesci/runtime.py (the ctypes stub of the integration guide) gives
+    every function of include/ofd.h an argument signature."""
+    syms = declared_symbols()
+    for name in syms:
+        fn = getattr(lib, name)
+        assert fn.argtypes is not None, name
