@@ -67,7 +67,9 @@ def rel_errors(got, ref, state_norm=False):
     return out
 
 
-@pytest.mark.parametrize('so,n,steps', [(4, 32, 100), (8, 32, 60), (2, 24, 60), (6, 24, 60)])
+@pytest.mark.parametrize('so,n,steps', [(4, 32, 100), (8, 32, 60), (2, 24, 60), (6, 24, 60),
+                                        # tests/eigenwave3d.py's case: 64^3 unit cube, SO4, 200 steps
+                                        (4, 64, 200)])
 def test_eigenwave_matches_oracle(tmp_path, so, n, steps):
     g = eigenwave_grid(grid_size=(n, n, n), ntsteps=steps, space_order=so)
     got = run_eigen_gpu(g)
