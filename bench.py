@@ -10,6 +10,11 @@ All inputs are synthetic and seeded.  The 18 field levels + 8 media arrays
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
+``--scheme acoustic`` measures the regular-grid (acoustic) scheme instead: the
+reference's tests/simplewaveequation.py model (one field, three time levels,
+its initialisation) on a 512^3 interior, space order 4, FP32; one step is one
+sweep (12 B of algorithmic traffic per grid point).
+
 Prints one JSON line.  Under torchrun each rank runs an independent replica
 (the path has no exchange step); value is the sum over ranks of grid-point
 updates divided by the slowest rank's time.
@@ -160,6 +165,143 @@ def run_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
+ACOUSTIC_METRIC = 'acoustic GLUP/s (grid-point updates per second), 512^3 SO4 FP32 regular grid'
+# reads u[t] and u[t-1], writes u[t+1]
+ACOUSTIC_BYTES_PER_LUP = 3 * 4
+
+
+def acoustic_problem(n, so, steps):
+    """The reference's acoustic model on an n^3 interior (unit cube split in
+    n intervals, grid_size n-1), its two initial levels: level 0 = 0 and
+    level 1 = v*dt on the interior (the reference's initialisation with
+    v = 1 on a zero level 0)."""
+    import numpy as np
+    from opesci.models import simplewave_grid
+    h = 1.0 / (n - 1)
+    g = simplewave_grid(grid_size=(n - 1,) * 3, dt=0.4 * h / (3 ** 0.5 * 2), tmax=1.0, space_order=so,
+                        ntsteps=steps)
+    dims = tuple(d.value for d in g.dim)
+    m = g.margin.value
+    l1 = np.zeros(dims, dtype=np.float32)
+    l1[m:-m, m:-m, m:-m] = np.float32(np.float32(1.0) * np.float32(g.dt.value))
+    return g, l1
+
+
+def acoustic_cpu(n, so, steps, threads=None):
+    from oracle import run as orun
+    from opesci.models import simplewave_grid
+    with tempfile.TemporaryDirectory() as d:
+        g = simplewave_grid(grid_size=(n - 1,) * 3, dt=0.4 / (n - 1) / (3 ** 0.5 * 2), tmax=1.0,
+                            space_order=so, ntsteps=steps)
+        out = orun.run_regular(g, d, threads=threads, dump=False)
+    return float(n) ** 3 * steps / out['loop_seconds'] / 1e9, out['threads'], out['loop_seconds']
+
+
+def run_acoustic(args, rank, world, local):
+    import numpy as np
+    from opesci import runtime, replicas
+
+    n, so = args.size, args.space_order
+    if args.impl == 'reference':
+        if rank != 0:
+            return
+        steps = max(1, min(args.steps, args.ref_steps))
+        val, cores, secs = acoustic_cpu(n, so, steps)
+        line = {'impl': 'reference', 'metric': ACOUSTIC_METRIC, 'value': val, 'unit': UNIT,
+                'n_gpus': args.gpus, 'steps': steps, 'warmup': 0, 'ms_per_step': secs * 1e3 / steps,
+                'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
+                'data': 'synthetic (the reference acoustic model and initialisation)',
+                'config': {'workload': 'acoustic %d^3 SO%d FP32' % (n, so), 'grid': [n, n, n], 'space_order': so},
+                'cpu_baseline': {'value': val, 'unit': UNIT, 'cores': cores, 'kind': 'port',
+                                 'sample': '%d steps, reference-shaped generated C++, time loop only' % steps},
+                'e2e': {'value': val, 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group('nccl')
+    runtime.set_device(local)
+    g, l1 = acoustic_problem(n, so, args.warmup + args.steps)
+    sim = runtime.RegularSimulation(runtime.regular_config_from_grid(g))
+    sim.upload(1, l1)
+    sim.step(args.warmup)
+    sim.sync()
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    if dist is not None:
+        dist.barrier()
+    sim.sync()
+    total_ms = sim.step_timed(args.steps)
+    if dist is not None:
+        dist.barrier()
+    clocks = sampler.stop()
+    lups_rank = float(n) ** 3 * args.steps
+    rate, secs = replicas.aggregate_rate(lups_rank, total_ms / 1e3, dist, device='cuda')
+    ms = secs * 1e3
+    peak, peak_src = measured_peak()
+    launch_ms = total_ms / args.steps
+    bytes_launch = float(n) ** 3 * ACOUSTIC_BYTES_PER_LUP
+    achieved = bytes_launch / (launch_ms / 1e3) / 1e9
+    tr = profiled_traffic('regular_sweep_so%d_f32' % so)
+    roofline = {'bound': 'hbm', 'kernel': 'regular sweep', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
+                'frac': achieved / peak, 'peak_source': peak_src,
+                'traffic': (tr * float(n) ** 3) if tr else None,
+                'algorithmic_bytes_per_launch': bytes_launch, 'avg_launch_ms': launch_ms}
+    e2e = None
+    if not args.no_e2e:
+        import torch
+        pin = lambda: torch.empty(sim.dims, dtype=torch.float32, pin_memory=True).numpy()  # noqa: E731
+        h0, h1, hout = pin(), pin(), pin()
+        h0[...] = 0.0
+        h1[...] = l1
+        sim.sync()
+        t0 = time.perf_counter()
+        sim.steps = 0
+        sim.upload(0, h0)
+        sim.upload(1, h1)
+        sim.step(args.steps)
+        sim.lib.ofd_regular_download(sim.h, sim.newest_level(), hout.ctypes.data)
+        sim.sync()
+        wall = time.perf_counter() - t0
+        cells = float(np.prod(sim.dims))
+        e2e = {'value': lups_rank / wall / 1e9, 'unit': UNIT,
+               'h2d_bytes_per_step': 2 * cells * 4 / args.steps, 'd2h_bytes_per_step': cells * 4 / args.steps,
+               'note': 'through the C ABI from pinned host buffers: two initial levels in, K steps, '
+                       'the newest level out'}
+    sim.close()
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        try:
+            # the bench's own grid, fewer steps (about 10 s on 16 cores)
+            csteps = max(1, min(args.cpu_steps, 100))
+            v, cores, csecs = acoustic_cpu(n, so, csteps)
+            cpu = {'value': v, 'unit': UNIT, 'cores': cores, 'kind': 'port',
+                   'sample': '%d steps of the %d^3 acoustic model, reference-shaped generated C++ '
+                             '(g++ -g -O3 -fno-tree-vectorize -fopenmp), time loop only, %.1f s'
+                             % (csteps, n, csecs)}
+        except Exception as e:  # report, do not hide
+            cpu = {'value': None, 'error': str(e)[:300]}
+    if rank == 0:
+        line = {'metric': ACOUSTIC_METRIC, 'value': rate / 1e9, 'unit': UNIT, 'n_gpus': world,
+                'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': ms / args.steps,
+                'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
+                'data': 'synthetic (the reference acoustic model and initialisation)',
+                'config': {'workload': 'acoustic %d^3 SO%d FP32 regular grid' % (n, so), 'grid': [n, n, n],
+                           'space_order': so, 'parallelism': 'replicas x%d' % world,
+                           'l2_flush': 'inputs larger than L2 (3 levels, %.1f GB)'
+                                       % (3 * float(np.prod(sim.dims)) * 4 / 1e9)},
+                'roofline': roofline, 'cpu_baseline': cpu, 'e2e': e2e, 'clocks': clocks,
+                'gpu_launches': args.steps}
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
@@ -176,9 +318,14 @@ def main():
     ap.add_argument('--cpu-steps', type=int, default=200)   # ~10 s of CPU work at 256^3
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--no-e2e', action='store_true')
+    ap.add_argument('--scheme', default='elastic', choices=['elastic', 'acoustic'])
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()
+
+    if args.scheme == 'acoustic':
+        run_acoustic(args, rank, world, local)
+        return
 
     if args.impl == 'reference':
         run_reference(args, rank)

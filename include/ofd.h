@@ -235,6 +235,56 @@ int ofd_field_view_get(ofd_handle *h, int field, int level, ofd_field_view *out)
 int ofd_sumsq_field_noalloc(const float *field, const int dims[3], int margin, double *out, void *stream);
 const char *ofd_noalloc_last_error(void);
 
+/* ------------------------------------------------------------------------
+ * Regular-grid (acoustic) scheme: one field, three time levels, the update
+ *
+ *     u[t+1](x,y,z) = sum_k coef[k] * u[t - 1 + level[k]](x+dx, y+dy, z+dz)
+ *
+ * that RegularGrid emits for a second-order-in-time equation
+ * (opesci/regulargrid.py:592-619 simple_kernel/kernel_sympy, time loop of
+ * opesci/templates/regular3d_tmpl.py:94-105, level rotation
+ * regulargrid.py:408-433).  Replaces the OpenMP time loop of that program.
+ *
+ * Terms are evaluated in the order given, as a left-to-right sum of
+ * products rounded in the storage type (acc = c0*v0; acc = acc + ck*vk; no
+ * fused multiply-add), which is how the reference's C expression
+ * "c0*u[..] + c1*u[..] - ..." rounds.  Coefficients are the values of the
+ * C literals (float literals, also in FP64 storage).  Offsets are bounded by
+ * the margin on every axis.  The handle counts steps ti: step ti writes level
+ * (ti%3 + 2)%3 from levels ti%3 (t-1) and (ti%3 + 1)%3 (t); margins are never
+ * written.  Host arrays use the layout real_t[dim1][dim2][dim3].
+ * ------------------------------------------------------------------------ */
+#define OFD_REGULAR_MAX_TERMS 96
+
+typedef struct ofd_regular_config {
+    int dim[3];          /* dim1, dim2, dim3 = interior points + 2*margin */
+    int margin;          /* space_order/2; the interior is [margin, dim-margin) */
+    int storage;         /* OFD_F32 or OFD_F64 */
+    int nterms;          /* 1..OFD_REGULAR_MAX_TERMS */
+    int level[OFD_REGULAR_MAX_TERMS];      /* 1: level t, 0: level t-1 */
+    int offset[OFD_REGULAR_MAX_TERMS][3];  /* dx, dy, dz, each in [-margin, margin] */
+    double coef[OFD_REGULAR_MAX_TERMS];    /* exact value of the C literal */
+} ofd_regular_config;
+
+typedef struct ofd_regular ofd_regular;
+
+/* three zeroed levels on the current device */
+int ofd_regular_create(const ofd_regular_config *cfg, ofd_regular **out);
+int ofd_regular_destroy(ofd_regular *h);
+/* one level, host or device array of real_t[dim1][dim2][dim3] */
+int ofd_regular_upload(ofd_regular *h, int level, const void *host);
+int ofd_regular_download(ofd_regular *h, int level, void *host);
+int ofd_regular_upload_device(ofd_regular *h, int level, const void *dev);
+int ofd_regular_download_device(ofd_regular *h, int level, void *dev);
+/* queue nsteps updates (one kernel each) on the handle's stream */
+int ofd_regular_step(ofd_regular *h, int nsteps);
+/* as ofd_regular_step, timed by CUDA events on the handle's stream; waits */
+int ofd_regular_step_timed(ofd_regular *h, int nsteps, double *ms);
+int ofd_regular_get_step(ofd_regular *h, long *steps);
+int ofd_regular_set_step(ofd_regular *h, long steps);
+int ofd_regular_sync(ofd_regular *h);
+void *ofd_regular_stream(ofd_regular *h);
+
 #ifdef __cplusplus
 }
 #endif

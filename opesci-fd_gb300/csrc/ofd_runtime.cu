@@ -27,6 +27,9 @@ static int fail(int code, const char *fmt, ...) {
   return code;
 }
 
+// for the other translation units of the library
+int fail_msg(int code, const char *msg) { return fail(code, "%s", msg); }
+
 #define OFD_CUDA(call)                                                                   \
   do {                                                                                   \
     cudaError_t _e = (call);                                                             \

@@ -126,14 +126,15 @@ class Grid(object):
 
     def field_array(self, name, level=None):
         """The published host array of a field after execute(), as NumPy
-        (reference layout [2][dim1][dim2][dim3]); ``level`` selects one level."""
+        (reference layout [levels][dim1][dim2][dim3]: two levels for the
+        elastic scheme, three for the regular one); ``level`` selects one."""
         import numpy as np
         if self._arg_grid is None:
             raise RuntimeError('run execute() first')
         dims = [d.value for d in self.dim]
         ptr = getattr(self._arg_grid, name)
         dtype = np.float64 if getattr(self, 'double', False) else np.float32
-        arr = np.ctypeslib.as_array(ptr, shape=(2,) + tuple(dims)).astype(dtype, copy=True)
+        arr = np.ctypeslib.as_array(ptr, shape=(len(self.time),) + tuple(dims)).astype(dtype, copy=True)
         return arr if level is None else arr[level]
 
     def free(self):

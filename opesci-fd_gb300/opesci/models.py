@@ -18,7 +18,7 @@ from .staggeredgrid import StaggeredGrid
 from .util import staggered_weights
 
 __all__ = ['eigenwave_grid', 'elastic_grid', 'layered_media', 'ricker',
-           'stable_dt', 'cfl_dt']
+           'stable_dt', 'cfl_dt', 'simplewave_grid']
 
 
 def _elastic_fields():
@@ -112,6 +112,34 @@ def eigenwave_grid(grid_size=(64, 64, 64), dt=None, ntsteps=200, space_order=4,
     # int(tmax/dt) may round down by one for some dt; pin the step count
     grid.ntsteps.value = ntsteps
     grid.legacy_bc = legacy
+    return grid
+
+
+def simplewave_grid(domain_size=(1.0, 1.0, 1.0), grid_size=(100, 100, 100), dt=0.002, tmax=1.0,
+                    space_order=4, double=False, ntsteps=None):
+    """The acoustic model of tests/simplewaveequation.py:9-81, built through
+    the public RegularGrid API: one RegularField, c = 2 and v = 1, the
+    analytic function -A sin(pi x)(sin(pi y) - sin(pi z)) sin(Omega t) with
+    mu = 10, beta = 0.5, and the model's equation as written there,
+    u_tt = c^2 (u_xx + u_yy + u_yy).  ``ntsteps`` overrides int(tmax/dt)."""
+    from .fields import RegularField
+    from .regulargrid import RegularGrid
+    main = RegularField('MAIN_GRID', dimension=3)
+    grid = RegularGrid(dimension=3, domain_size=domain_size, grid_size=grid_size, fields=[main])
+    grid.set_time_step(dt, tmax)
+    if ntsteps is not None:
+        grid.ntsteps.value = int(ntsteps)
+    grid.set_switches(double=double, expand=True, eval_const=True, converge=True)
+    t, x, y, z, c = symbols('_t x y z c')
+    grid.set_index([x, y, z])
+    grid.set_params(c=2, v=1)
+    mu, beta = 10, 0.5
+    Omega = pi * sqrt(2 * mu * beta)
+    A = sqrt(2 * mu / beta)
+    main.set_analytic_solution(-A * sin(pi * x) * (sin(pi * y) - sin(pi * z)) * sin(Omega * t))
+    grid.set_order([2, space_order, space_order, space_order])
+    grid.calc_derivatives(2)
+    grid.solve_fd([Eq(main.d[0][2], (c ** 2) * (main.d[1][2] + main.d[2][2] + main.d[2][2]))])
     return grid
 
 

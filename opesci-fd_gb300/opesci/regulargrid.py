@@ -67,8 +67,10 @@ class RegularGrid(Grid):
 
     # ------------------------------------------------------------------ setup
     def initialize_template(self):
-        """The CUDA program template for this grid (set by subclasses)."""
-        self.cgen_template = None
+        """The CUDA program template of the acoustic scheme (StaggeredGrid
+        overrides it with the elastic one)."""
+        from .templates.regular_tmpl import RegularCudaTemplate
+        self.cgen_template = RegularCudaTemplate(self)
 
     def set_variable(self, var, value=0, type='int', constant=False):
         """Define a named constant/variable of the generated program
@@ -241,6 +243,42 @@ class RegularGrid(Grid):
         if self.eval_const:
             kernel_new = kernel_new.subs(self.const_dict)
         return kernel_new
+
+    def kernel_sympy(self, field):
+        """Transformed kernel with t+1 -> t2, t -> t1, t-1 -> t0
+        (regulargrid.py:592-595)."""
+        if self.eval_const:
+            self.create_const_dict()
+        kernel = self.transform_kernel(field)
+        return kernel.xreplace({self.t + 1: self.time[2], self.t: self.time[1], self.t - 1: self.time[0]})
+
+    def initial_kernel(self, field):
+        """Right-hand side of the first initialisation, level 0 on the whole
+        padded grid (regulargrid.py:498-534): the analytic solution at t = 0
+        with the loop indices _x, _y, _z substituted for the coordinates, as
+        the reference does."""
+        sol = field.sol.subs(self.t, 0)
+        for idx in self.index:
+            sol = sol.subs(idx, '_' + idx.name)
+        return sol
+
+    def second_initial_kernel(self, field):
+        """Right-hand side of the second initialisation, level _t1 on the
+        interior (regulargrid.py:536-564): the update kernel with its
+        negative t-1 term dropped, halved, plus v*dt, read at level _t0."""
+        v = Symbol('v')
+        if self.eval_const:
+            self.create_const_dict()
+        kernel = self.transform_kernel(field)
+        for arg in kernel.args:
+            if str(arg).startswith('-') and str(self.t - 1) in str(arg):
+                kernel = kernel.subs({arg: 0}, simultaneous=True)
+                arg = 2 * v * self.dt
+                kernel = 0.5 * (kernel + arg)
+        kernel = kernel.subs({self.t: self.time[0]})
+        for idx in self.index:
+            kernel = kernel.subs(idx, '_' + idx.name)
+        return kernel
 
     def set_papi_events(self, events=[]):
         self._papi_events = events

@@ -11,7 +11,8 @@ import numpy as np
 from . import build as _build
 
 __all__ = ['OFDError', 'load_library', 'Simulation', 'FIELDS', 'STORAGE', 'BC',
-           'config_from_grid', 'library_path']
+           'config_from_grid', 'library_path', 'RegularSimulation', 'regular_config',
+           'regular_config_from_grid']
 
 FIELDS = ['U', 'V', 'W', 'Txx', 'Tyy', 'Tzz', 'Txy', 'Tyz', 'Txz']
 STORAGE = {'f32': 0, 'float': 0, 'fp32': 0, 'f16': 1, 'fp16': 1, 'half': 1,
@@ -34,6 +35,19 @@ class ofd_config(ctypes.Structure):
                 ('weights', ctypes.c_double * 4),
                 ('field_scale', ctypes.c_float * 9),
                 ('kernel_variant', ctypes.c_int)]
+
+
+REGULAR_MAX_TERMS = 96
+
+
+class ofd_regular_config(ctypes.Structure):
+    _fields_ = [('dim', ctypes.c_int * 3),
+                ('margin', ctypes.c_int),
+                ('storage', ctypes.c_int),
+                ('nterms', ctypes.c_int),
+                ('level', ctypes.c_int * REGULAR_MAX_TERMS),
+                ('offset', (ctypes.c_int * 3) * REGULAR_MAX_TERMS),
+                ('coef', ctypes.c_double * REGULAR_MAX_TERMS)]
 
 
 class ofd_field_view(ctypes.Structure):
@@ -100,6 +114,17 @@ def load_library():
         'ofd_group_query': [h],
         'ofd_group_sync': [h],
         'ofd_group_destroy': [h],
+        'ofd_regular_create': [P(ofd_regular_config), P(h)],
+        'ofd_regular_destroy': [h],
+        'ofd_regular_upload': [h, ctypes.c_int, ctypes.c_void_p],
+        'ofd_regular_download': [h, ctypes.c_int, ctypes.c_void_p],
+        'ofd_regular_upload_device': [h, ctypes.c_int, ctypes.c_void_p],
+        'ofd_regular_download_device': [h, ctypes.c_int, ctypes.c_void_p],
+        'ofd_regular_step': [h, ctypes.c_int],
+        'ofd_regular_step_timed': [h, ctypes.c_int, P(ctypes.c_double)],
+        'ofd_regular_get_step': [h, P(ctypes.c_long)],
+        'ofd_regular_set_step': [h, ctypes.c_long],
+        'ofd_regular_sync': [h],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -109,6 +134,8 @@ def load_library():
     lib.ofd_last_error.restype = ctypes.c_char_p
     lib.ofd_stream.argtypes = [h]
     lib.ofd_stream.restype = ctypes.c_void_p
+    lib.ofd_regular_stream.argtypes = [h]
+    lib.ofd_regular_stream.restype = ctypes.c_void_p
     lib.ofd_sumsq_field_noalloc.argtypes = [ctypes.c_void_p, P(ctypes.c_int), ctypes.c_int, ctypes.c_void_p,
                                             ctypes.c_void_p]
     lib.ofd_sumsq_field_noalloc.restype = ctypes.c_int
@@ -423,6 +450,110 @@ class Group(object):
         if self.g:
             self.lib.ofd_group_destroy(self.g)
             self.g = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+# --------------------------------------------------------------- regular grid
+
+def regular_config(dims, margin, terms, storage='f32'):
+    """ofd_regular_config from padded dims, the margin and a term table
+    [(level, (dx, dy, dz), coef), ...] (level 1: t, 0: t-1)."""
+    st = {'f32': 0, 'float': 0, 'fp32': 0, 'f64': 3, 'double': 3, 'fp64': 3}.get(storage)
+    if st is None:
+        raise ValueError('regular-grid storage must be f32 or f64, not %r' % storage)
+    if not 1 <= len(terms) <= REGULAR_MAX_TERMS:
+        raise ValueError('%d terms (1..%d supported)' % (len(terms), REGULAR_MAX_TERMS))
+    cfg = ofd_regular_config()
+    for i in range(3):
+        cfg.dim[i] = int(dims[i])
+    cfg.margin = int(margin)
+    cfg.storage = st
+    cfg.nterms = len(terms)
+    for k, (lvl, off, coef) in enumerate(terms):
+        cfg.level[k] = int(lvl)
+        for d in range(3):
+            cfg.offset[k][d] = int(off[d])
+        cfg.coef[k] = float(coef)
+    return cfg
+
+
+def regular_config_from_grid(grid):
+    """The device configuration of a solved one-field RegularGrid."""
+    from .templates.regular_tmpl import regular_terms
+    if len(grid.fields) != 1:
+        raise ValueError('the regular-grid device runtime advances one field')
+    terms = regular_terms(grid, grid.fields[0])
+    return regular_config([d.value for d in grid.dim], grid.margin.value, terms,
+                          'f64' if grid.double else 'f32')
+
+
+class RegularSimulation(object):
+    """One regular-grid (acoustic) field on three time levels resident in HBM
+    (ofd_regular_*).  Level arrays are real_t[dim1][dim2][dim3]; step n
+    writes level (n % 3 + 2) % 3 from levels n % 3 (t-1) and (n % 3 + 1) % 3
+    (t), like the reference's _t0/_t1/_t2 rotation."""
+
+    def __init__(self, cfg):
+        self.lib = load_library()
+        self.cfg = cfg
+        self.dims = tuple(cfg.dim)
+        self.dtype = np.float64 if cfg.storage == 3 else np.float32
+        self.h = ctypes.c_void_p()
+        _check(self.lib.ofd_regular_create(ctypes.byref(cfg), ctypes.byref(self.h)), 'ofd_regular_create')
+
+    def upload(self, level, arr):
+        a = np.ascontiguousarray(arr, dtype=self.dtype)
+        if a.shape != self.dims:
+            raise ValueError('level shape %s, expected %s' % (a.shape, self.dims))
+        _check(self.lib.ofd_regular_upload(self.h, int(level), a.ctypes.data), 'ofd_regular_upload')
+
+    def download(self, level):
+        a = np.empty(self.dims, dtype=self.dtype)
+        _check(self.lib.ofd_regular_download(self.h, int(level), a.ctypes.data), 'ofd_regular_download')
+        return a
+
+    def step(self, n):
+        _check(self.lib.ofd_regular_step(self.h, int(n)), 'ofd_regular_step')
+
+    def step_timed(self, n):
+        """Milliseconds of n steps measured by CUDA events on the handle's stream."""
+        ms = ctypes.c_double()
+        _check(self.lib.ofd_regular_step_timed(self.h, int(n), ctypes.byref(ms)), 'ofd_regular_step_timed')
+        return ms.value
+
+    @property
+    def steps(self):
+        v = ctypes.c_long()
+        _check(self.lib.ofd_regular_get_step(self.h, ctypes.byref(v)), 'ofd_regular_get_step')
+        return v.value
+
+    @steps.setter
+    def steps(self, n):
+        _check(self.lib.ofd_regular_set_step(self.h, int(n)), 'ofd_regular_set_step')
+
+    def newest_level(self):
+        """Level written by the last step (level 1 before any step)."""
+        n = self.steps
+        return 1 if n == 0 else ((n - 1) % 3 + 2) % 3
+
+    def sync(self):
+        _check(self.lib.ofd_regular_sync(self.h), 'ofd_regular_sync')
+
+    def close(self):
+        if self.h:
+            self.lib.ofd_regular_destroy(self.h)
+            self.h = ctypes.c_void_p()
 
     def __del__(self):
         try:

@@ -13,7 +13,7 @@ import subprocess
 
 import numpy as np
 
-from . import cpp_emitter
+from . import cpp_emitter, regular_emitter
 
 # -ffp-contract=off states what g++ already does for ISO C++ on x86-64 (no
 # FMA contraction), so the program rounds the same on the aarch64 GPU hosts
@@ -70,4 +70,36 @@ def run(grid, workdir, legacy=False, source=None, threads=None, vectorize=False,
         if receivers:
             out['traces'] = np.fromfile(prefix + 'traces.raw', dtype=np.float32).reshape(
                 grid.ntsteps.value, 4, len(receivers))
+    return out
+
+
+def run_regular(grid, workdir, threads=None, vectorize=False, dump=True):
+    """Emit, compile and run the oracle program of a RegularGrid (acoustic
+    scheme).  Returns 'l2', 'l2_fp64', 'loop_seconds', 'threads' and
+    'levels' ({field: array[3][dim1][dim2][dim3]}, all three time levels)."""
+    workdir = os.path.abspath(workdir)
+    prefix = os.path.join(workdir, "rdump_") if dump else None
+    src = regular_emitter.generate(grid, dump_prefix=prefix)
+    exe = compile_program(src, workdir, vectorize=vectorize)
+    env = dict(os.environ)
+    nthreads = threads or os.cpu_count() or 1
+    env['OMP_NUM_THREADS'] = str(nthreads)
+    env['OMP_PROC_BIND'] = 'close'
+    r = subprocess.run([exe], capture_output=True, text=True, env=env, cwd=workdir)
+    if r.returncode != 0:
+        raise RuntimeError('oracle run failed (%d): %s' % (r.returncode, r.stderr[-2000:]))
+    out = {'l2': {}, 'l2_fp64': {}, 'loop_seconds': None, 'threads': nthreads, 'stdout': r.stdout}
+    for line in r.stdout.splitlines():
+        p = line.split()
+        if p and p[0] == 'loop_seconds':
+            out['loop_seconds'] = float(p[1])
+        elif p and p[0].endswith('_l2') and len(p) >= 3:
+            out['l2'][p[0][:-3]] = float(p[1])
+            out['l2_fp64'][p[0][:-3]] = float(p[2])
+    if dump:
+        from opesci.codeprinter import ccode
+        dims = (len(grid.time),) + tuple(d.value for d in grid.dim)
+        real = np.float64 if grid.double else np.float32
+        out['levels'] = {ccode(f.label): np.fromfile(prefix + ccode(f.label) + '.raw', dtype=real).reshape(dims)
+                         for f in grid.fields}
     return out
