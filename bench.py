@@ -226,7 +226,7 @@ def run_acoustic(args, rank, world, local):
         dist.init_process_group('nccl')
     runtime.set_device(local)
     g, l1 = acoustic_problem(n, so, args.warmup + args.steps)
-    sim = runtime.RegularSimulation(runtime.regular_config_from_grid(g))
+    sim = runtime.RegularSimulation(runtime.regular_config_from_grid(g, variant=args.variant))
     sim.upload(1, l1)
     sim.step(args.warmup)
     sim.sync()
@@ -247,8 +247,9 @@ def run_acoustic(args, rank, world, local):
     launch_ms = total_ms / args.steps
     bytes_launch = float(n) ** 3 * ACOUSTIC_BYTES_PER_LUP
     achieved = bytes_launch / (launch_ms / 1e3) / 1e9
-    tr = profiled_traffic('regular_sweep_so%d_f32' % so)
-    roofline = {'bound': 'hbm', 'kernel': 'regular sweep', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
+    tr = profiled_traffic('regular_sweep_so%d_f32_v%d' % (so, args.variant))
+    roofline = {'bound': 'hbm', 'kernel': 'regular sweep (%s)' % ('direct', 'shared-memory ring')[args.variant],
+                'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
                 'frac': achieved / peak, 'peak_source': peak_src,
                 'traffic': (tr * float(n) ** 3) if tr else None,
                 'algorithmic_bytes_per_launch': bytes_launch, 'avg_launch_ms': launch_ms}
@@ -294,7 +295,8 @@ def run_acoustic(args, rank, world, local):
                 'config': {'workload': 'acoustic %d^3 SO%d FP32 regular grid' % (n, so), 'grid': [n, n, n],
                            'space_order': so, 'parallelism': 'replicas x%d' % world,
                            'l2_flush': 'inputs larger than L2 (3 levels, %.1f GB)'
-                                       % (3 * float(np.prod(sim.dims)) * 4 / 1e9)},
+                                       % (3 * float(np.prod(sim.dims)) * 4 / 1e9),
+                           'kernel_variant': args.variant},
                 'roofline': roofline, 'cpu_baseline': cpu, 'e2e': e2e, 'clocks': clocks,
                 'gpu_launches': args.steps}
         print(json.dumps(line), flush=True)

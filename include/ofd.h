@@ -264,6 +264,7 @@ typedef struct ofd_regular_config {
     int level[OFD_REGULAR_MAX_TERMS];      /* 1: level t, 0: level t-1 */
     int offset[OFD_REGULAR_MAX_TERMS][3];  /* dx, dy, dz, each in [-margin, margin] */
     double coef[OFD_REGULAR_MAX_TERMS];    /* exact value of the C literal */
+    int variant;         /* 0: direct sweep (default), 1: shared-memory ring sweep */
 } ofd_regular_config;
 
 typedef struct ofd_regular ofd_regular;

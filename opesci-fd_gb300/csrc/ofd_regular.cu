@@ -6,8 +6,10 @@
 // u[_t2] = f(u[_t1], u[_t0]) on the interior, margins never written).
 //
 // HBM-bound: per interior point the sweep reads u[t] and u[t-1] once and
-// writes u[t+1] once (12 B/LUP in FP32).  A CTA owns a 32(z) x 8(y) column
-// tile and walks a chunk of x planes.  Level t is staged in a shared-memory
+// writes u[t+1] once (12 B/LUP in FP32).  Two variants: a direct one (the
+// default, below) and a shared-memory ring.  In both a CTA owns a 32(z) x
+// 8(y) column tile and walks a chunk of x planes.  In the ring variant,
+// level t is staged in a shared-memory
 // ring of 2R+1 planes of the tile plus an R-wide halo, so each value of u[t]
 // is read from memory once per CTA and every stencil term of the table is a
 // shared-memory read; level t-1 terms read global memory directly.  Terms
@@ -132,6 +134,36 @@ __global__ void __launch_bounds__(NT) regular_sweep_kernel(const RegSweep<T> a) 
   }
 }
 
+// Direct variant: no shared memory and no barriers.  Each thread walks a
+// chunk of x planes of one (y, z) column and reads every term through the
+// read-only path; neighbours along z and y come from the same or nearby
+// warps' lines in L1, neighbours along x from planes this thread read a few
+// iterations earlier, so memory traffic stays near the algorithmic 12 B/LUP
+// while every warp is independent (latency is hidden by occupancy, not by
+// a pipeline).
+template <typename T>
+__global__ void __launch_bounds__(NT) regular_direct_kernel(const RegSweep<T> a) {
+  const int z = a.m + blockIdx.x * TZ + threadIdx.x;
+  const int y = a.m + blockIdx.y * TY + threadIdx.y;
+  if (z >= a.n3 - a.m || y >= a.n2 - a.m) return;
+  const int xb = a.m + blockIdx.z * a.chunk;
+  const int xe = min(xb + a.chunk, a.n1 - a.m);
+  const T *__restrict__ cur = a.cur;
+  const T *__restrict__ prev = a.prev;
+  T *__restrict__ next = a.next;
+  long g = (long)xb * a.plane + (long)y * a.P + z;
+  for (int x = xb; x < xe; ++x, g += a.plane) {
+    T acc = T(0);
+#pragma unroll 8
+    for (int k = 0; k < a.nterms; ++k) {
+      const T *base = a.lvl[k] ? cur : prev;
+      const T p = mul_rn(a.coef[k], __ldg(base + g + a.goff[k]));
+      acc = k ? add_rn(acc, p) : p;
+    }
+    next[g] = acc;
+  }
+}
+
 size_t esize_of(int storage) { return storage == OFD_F64 ? 8 : storage == OFD_F32 ? 4 : 0; }
 
 size_t ring_bytes(int m, size_t es) {
@@ -152,6 +184,7 @@ struct ofd_regular {
   long level = 0;      // elements per level (256-B multiple)
   long ti = 0;         // steps done
   int chunk = 8;
+  int variant = 0;     // 0: direct, 1: shared-memory ring
   dim3 grid;
   size_t smem = 0;
   RegSweep<float> a32[3];    // by ti % 3
@@ -204,6 +237,7 @@ int check(const ofd_regular_config *c) {
     if (c->dim[i] < 2 * c->margin + 1) return rfail(OFD_EINVAL, "dim%d = %d has no interior", i + 1, c->dim[i]);
     if (c->dim[i] > (1 << 15)) return rfail(OFD_EINVAL, "dim%d = %d too large", i + 1, c->dim[i]);
   }
+  if (c->variant < 0 || c->variant > 1) return rfail(OFD_EINVAL, "variant %d outside [0, 1]", c->variant);
   if (c->nterms < 1 || c->nterms > OFD_REGULAR_MAX_TERMS)
     return rfail(OFD_EINVAL, "nterms %d outside [1, %d]", c->nterms, OFD_REGULAR_MAX_TERMS);
   for (int k = 0; k < c->nterms; ++k) {
@@ -256,17 +290,24 @@ int ofd_regular_create(const ofd_regular_config *cfg, ofd_regular **out) {
   h->level = ((long)cfg->dim[0] * h->plane + al - 1) / al * al;
   const int nx = cfg->dim[0] - 2 * m, ny = cfg->dim[1] - 2 * m, nz = cfg->dim[2] - 2 * m;
   const long tiles = (long)((nz + TZ - 1) / TZ) * ((ny + TY - 1) / TY);
-  // about eight waves of 8 resident CTAs on each of the GPU's SMs
-  int sms = 152;
-  int dev = 0;
-  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const long want = (long)sms * 8 * 8;
-  long chunk = ((long)nx * tiles + want - 1) / want;
-  if (chunk < 8) chunk = 8;
+  h->variant = cfg->variant;
+  long chunk;
+  if (h->variant == 0) {
+    // short columns: x neighbours are still in L1 when a thread reaches them
+    chunk = 16;
+  } else {
+    // about eight waves of 8 resident CTAs on each of the GPU's SMs
+    int sms = 152;
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long want = (long)sms * 8 * 8;
+    chunk = ((long)nx * tiles + want - 1) / want;
+    if (chunk < 8) chunk = 8;
+  }
   if (chunk > nx) chunk = nx;
   h->chunk = (int)chunk;
   h->grid = dim3((nz + TZ - 1) / TZ, (ny + TY - 1) / TY, (nx + h->chunk - 1) / h->chunk);
-  h->smem = ring_bytes(m, h->es);
+  h->smem = h->variant == 1 ? ring_bytes(m, h->es) : 0;
   cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMalloc(&h->raw, (size_t)h->level * 3 * h->es);
   if (e == cudaSuccess) e = cudaMemsetAsync(h->raw, 0, (size_t)h->level * 3 * h->es, h->stream);
@@ -323,10 +364,17 @@ int ofd_regular_step(ofd_regular *h, int nsteps) {
   if (nsteps < 0) return rfail(OFD_EINVAL, "nsteps must be >= 0");
   for (int s = 0; s < nsteps; ++s, ++h->ti) {
     const int r = (int)(h->ti % 3);
-    if (h->es == 4)
-      regular_sweep_kernel<float><<<h->grid, dim3(TZ, TY), h->smem, h->stream>>>(h->a32[r]);
-    else
-      regular_sweep_kernel<double><<<h->grid, dim3(TZ, TY), h->smem, h->stream>>>(h->a64[r]);
+    if (h->variant == 0) {
+      if (h->es == 4)
+        regular_direct_kernel<float><<<h->grid, dim3(TZ, TY), 0, h->stream>>>(h->a32[r]);
+      else
+        regular_direct_kernel<double><<<h->grid, dim3(TZ, TY), 0, h->stream>>>(h->a64[r]);
+    } else {
+      if (h->es == 4)
+        regular_sweep_kernel<float><<<h->grid, dim3(TZ, TY), h->smem, h->stream>>>(h->a32[r]);
+      else
+        regular_sweep_kernel<double><<<h->grid, dim3(TZ, TY), h->smem, h->stream>>>(h->a64[r]);
+    }
     REG_CUDA(cudaGetLastError());
   }
   return OFD_OK;

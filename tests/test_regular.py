@@ -100,26 +100,27 @@ def test_generated_program_compiles(tmp_path):
 
 # ----------------------------------------------------------------- GPU
 
-def _levels_sim(g, ref0):
+def _levels_sim(g, ref0, variant=0):
     """RegularSimulation holding the oracle's initial levels."""
     from opesci import runtime
-    sim = runtime.RegularSimulation(runtime.regular_config_from_grid(g))
+    sim = runtime.RegularSimulation(runtime.regular_config_from_grid(g, variant=variant))
     for lvl in range(3):
         sim.upload(lvl, ref0[lvl])
     return sim
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize('variant', [0, 1])
 @pytest.mark.parametrize('so,double,shape', [(2, False, (37, 29, 45)), (4, False, (37, 29, 45)),
                                              (8, False, (33, 41, 30)), (4, True, (25, 31, 27)),
                                              (16, False, (40, 24, 36))])
-def test_device_sweep_matches_oracle(tmp_path, so, double, shape):
+def test_device_sweep_matches_oracle(tmp_path, so, double, shape, variant):
     g = simplewave_grid(grid_size=shape, space_order=so, ntsteps=0, double=double)
     ref0 = orun.run_regular(g, str(tmp_path / 'r0'), threads=4)['levels']['MAIN_GRID']
     steps = 11
     g.ntsteps.value = steps
     ref = orun.run_regular(g, str(tmp_path / 'rn'), threads=4)['levels']['MAIN_GRID']
-    sim = _levels_sim(g, ref0)
+    sim = _levels_sim(g, ref0, variant)
     sim.step(steps)
     sim.sync()
     assert sim.steps == steps
@@ -153,7 +154,8 @@ def test_device_config_validation_without_gpu():
     build.build()
     for cfg, msg in ((runtime.regular_config((20, 20, 20), 2, [(1, (3, 0, 0), 1.0)]), 'margin'),
                      (runtime.regular_config((20, 20, 20), 9, [(1, (0, 0, 0), 1.0)]), 'margin'),
-                     (runtime.regular_config((4, 20, 20), 2, [(1, (0, 0, 0), 1.0)]), 'interior')):
+                     (runtime.regular_config((4, 20, 20), 2, [(1, (0, 0, 0), 1.0)]), 'interior'),
+                     (runtime.regular_config((20, 20, 20), 2, [(1, (0, 0, 0), 1.0)], variant=2), 'variant')):
         with pytest.raises(runtime.OFDError, match=msg):
             runtime.RegularSimulation(cfg)
     with pytest.raises(ValueError):
