@@ -130,7 +130,11 @@ def build_problem(n, so, steps, seed=0):
     return layered_problem(n, space_order=so, ntsteps=steps, seed=seed)
 
 
-def cpu_oracle(n, so, steps, seed=0, threads=None):
+def cpu_flags(vectorize):
+    return '-O3 -fopenmp' if vectorize else '-g -O3 -fno-tree-vectorize -fopenmp'
+
+
+def cpu_oracle(n, so, steps, seed=0, threads=None, vectorize=False):
     """Time the reference-shaped generated C++ (the oracle program: the
     reference's generator output for this model, reference GNU flags) on the
     host cores for ``steps`` steps of an n^3 problem of the same kind."""
@@ -139,7 +143,7 @@ def cpu_oracle(n, so, steps, seed=0, threads=None):
     with tempfile.TemporaryDirectory() as d:
         files = {k: os.path.join(d, k + '.raw') for k in ('rho', 'vp', 'vs')}
         g, media, src, wav = layered_problem(n, space_order=so, ntsteps=steps, seed=seed, media_files=files)
-        out = orun.run(g, d, source=(src, wav), threads=threads, dump=False)
+        out = orun.run(g, d, source=(src, wav), threads=threads, dump=False, vectorize=vectorize)
     lups = float(n) ** 3 * steps
     return lups / out['loop_seconds'] / 1e9, out['threads'], out['loop_seconds']
 
@@ -149,7 +153,7 @@ def run_reference(args, rank):
         return
     n = args.size if args.ref_size is None else args.ref_size
     steps = max(1, min(args.steps, args.ref_steps))
-    val, cores, secs = cpu_oracle(n, args.space_order, steps)
+    val, cores, secs = cpu_oracle(n, args.space_order, steps, vectorize=args.cpu_vectorize)
     line = {
         'impl': 'reference', 'metric': METRIC, 'value': val, 'unit': UNIT,
         'n_gpus': args.gpus, 'steps': steps, 'warmup': 0, 'ms_per_step': secs * 1e3 / steps,
@@ -159,7 +163,7 @@ def run_reference(args, rank):
                    'grid': [n, n, n], 'space_order': args.space_order, 'l2_flush': 'inputs larger than L2'},
         'cpu_baseline': {'value': val, 'unit': UNIT, 'cores': cores, 'kind': 'port',
                          'sample': '%d steps of the %d^3 problem, reference-shaped generated C++ '
-                                   '(g++ -g -O3 -fno-tree-vectorize -fopenmp), time loop only' % (steps, n)},
+                                   '(g++ %s), time loop only' % (steps, n, cpu_flags(args.cpu_vectorize))},
         'e2e': {'value': val, 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
     }
     print(json.dumps(line), flush=True)
@@ -187,13 +191,13 @@ def acoustic_problem(n, so, steps):
     return g, l1
 
 
-def acoustic_cpu(n, so, steps, threads=None):
+def acoustic_cpu(n, so, steps, threads=None, vectorize=False):
     from oracle import run as orun
     from opesci.models import simplewave_grid
     with tempfile.TemporaryDirectory() as d:
         g = simplewave_grid(grid_size=(n - 1,) * 3, dt=0.4 / (n - 1) / (3 ** 0.5 * 2), tmax=1.0,
                             space_order=so, ntsteps=steps)
-        out = orun.run_regular(g, d, threads=threads, dump=False)
+        out = orun.run_regular(g, d, threads=threads, dump=False, vectorize=vectorize)
     return float(n) ** 3 * steps / out['loop_seconds'] / 1e9, out['threads'], out['loop_seconds']
 
 
@@ -206,14 +210,15 @@ def run_acoustic(args, rank, world, local):
         if rank != 0:
             return
         steps = max(1, min(args.steps, args.ref_steps))
-        val, cores, secs = acoustic_cpu(n, so, steps)
+        val, cores, secs = acoustic_cpu(n, so, steps, vectorize=args.cpu_vectorize)
         line = {'impl': 'reference', 'metric': ACOUSTIC_METRIC, 'value': val, 'unit': UNIT,
                 'n_gpus': args.gpus, 'steps': steps, 'warmup': 0, 'ms_per_step': secs * 1e3 / steps,
                 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
                 'data': 'synthetic (the reference acoustic model and initialisation)',
                 'config': {'workload': 'acoustic %d^3 SO%d FP32' % (n, so), 'grid': [n, n, n], 'space_order': so},
                 'cpu_baseline': {'value': val, 'unit': UNIT, 'cores': cores, 'kind': 'port',
-                                 'sample': '%d steps, reference-shaped generated C++, time loop only' % steps},
+                                 'sample': '%d steps, reference-shaped generated C++ (g++ %s), time loop only'
+                                           % (steps, cpu_flags(args.cpu_vectorize))},
                 'e2e': {'value': val, 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
         print(json.dumps(line), flush=True)
         return
@@ -321,6 +326,9 @@ def main():
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--scheme', default='elastic', choices=['elastic', 'acoustic'])
+    # reference arm only: g++ -O3 -fopenmp with vectorisation on instead of
+    # the reference's own -fno-tree-vectorize build flags
+    ap.add_argument('--cpu-vectorize', action='store_true')
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()
