@@ -60,6 +60,35 @@ def test_term_table_matches_reference_program(tmp_path, so):
     assert np.abs(want).max() > 0
 
 
+def test_coefficient_values_follow_c_literals():
+    """Coefficients take the value the C compiler gives the printed literal:
+    float literals rounded once to float32, integers exactly, p.0F/q.0F as a
+    float32 division."""
+    from fractions import Fraction
+    from opesci.templates.regular_tmpl import _coef_value
+    for lit in ('2.13333333333333e-1', '1.33333333333333e-2', '8.0e-1', '1.06666666666667e-1'):
+        f = _coef_value(lit + 'F')
+        q = Fraction(lit)
+        up = np.nextafter(f, np.float32(np.inf))
+        down = np.nextafter(f, np.float32(-np.inf))
+        # nearest float32 to the decimal value
+        assert abs(Fraction(float(f)) - q) <= min(abs(Fraction(float(up)) - q), abs(Fraction(float(down)) - q))
+    assert _coef_value('2') == np.float32(2)
+    assert _coef_value('1.0F/12.0F') == np.float32(1) / np.float32(12)
+    with pytest.raises(ValueError):
+        _coef_value('dt')
+
+
+def test_fp64_table_keeps_float_literals():
+    """With double=True the printed literals still carry the F suffix, so the
+    FP64 program multiplies by float32 values; the table is the FP32 one."""
+    a = regular_terms(*(lambda g: (g, g.fields[0]))(simplewave_grid(grid_size=(12, 12, 12), ntsteps=2)))
+    b = regular_terms(*(lambda g: (g, g.fields[0]))(simplewave_grid(grid_size=(12, 12, 12), ntsteps=2,
+                                                                   double=True)))
+    assert a == b
+    assert all(float(np.float32(c)) == c for _, _, c in a)
+
+
 def test_term_table_rejects_unexpanded_kernels():
     g = simplewave_grid(grid_size=(10, 10, 10), space_order=4, ntsteps=2)
     g.expand = False
