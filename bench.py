@@ -134,6 +134,48 @@ def cpu_flags(vectorize):
     return '-O3 -fopenmp' if vectorize else '-g -O3 -fno-tree-vectorize -fopenmp'
 
 
+def cpu_model():
+    """Host CPU model name (lscpu, else /proc/cpuinfo), for the baseline record."""
+    try:
+        out = subprocess.run(['lscpu'], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith('model name'):
+                return line.split(':', 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in open('/proc/cpuinfo'):
+            if line.lower().startswith('model name'):
+                return line.split(':', 1)[1].strip()
+    except OSError:
+        pass
+    return 'unknown'
+
+
+def elastic_config(n, so, storage, world, variant, footprint_gb=None):
+    """The config dict both arms print for the elastic workload."""
+    return {'workload': 'elastic %d^3 SO%d %s heterogeneous + Ricker source, free surfaces'
+                        % (n, so, storage.upper()),
+            'grid': [n, n, n], 'space_order': so, 'storage': storage,
+            'parallelism': 'replicas x%d' % world,
+            'l2_flush': 'inputs larger than L2' + (' (%.1f GB resident)' % footprint_gb if footprint_gb else ''),
+            'kernel_variant': variant}
+
+
+def cpu_baseline_pair(n, so, steps, threads=None):
+    """Both CPU builds of the oracle program on the same bounded sample: the
+    stated baseline is g++ -O3 -fopenmp (vectorisation on); the reference's
+    own GNU flags (-fno-tree-vectorize) are reported beside it."""
+    v_vec, cores, s_vec = cpu_oracle(n, so, steps, threads=threads, vectorize=True)
+    v_ref, _, s_ref = cpu_oracle(n, so, steps, threads=threads, vectorize=False)
+    return {'value': v_vec, 'unit': UNIT, 'cores': cores, 'kind': 'port',
+            'cpu_model': cpu_model(), 'omp_proc_bind': 'close',
+            'sample': '%d steps of a %d^3 problem of the same kind (SO%d, heterogeneous, source), '
+                      'reference-shaped generated C++ (g++ -O3 -fopenmp), time loop only, %.1f s'
+                      % (steps, n, so, s_vec),
+            'reference_flags': {'value': v_ref, 'flags': cpu_flags(False), 'seconds': s_ref}}
+
+
 def cpu_oracle(n, so, steps, seed=0, threads=None, vectorize=False):
     """Time the reference-shaped generated C++ (the oracle program: the
     reference's generator output for this model, reference GNU flags) on the
@@ -149,21 +191,32 @@ def cpu_oracle(n, so, steps, seed=0, threads=None, vectorize=False):
 
 
 def run_reference(args, rank):
+    """The reference arm: the oracle program (the reference-shaped generated
+    C++) on the bench's own workload, all host threads, both builds: g++ -O3
+    -fopenmp (the stated value) and the reference's GNU flags beside it."""
     if rank != 0:
         return
     n = args.size if args.ref_size is None else args.ref_size
     steps = max(1, min(args.steps, args.ref_steps))
-    val, cores, secs = cpu_oracle(n, args.space_order, steps, vectorize=args.cpu_vectorize)
+    vec = not args.cpu_reference_flags
+    val, cores, secs = cpu_oracle(n, args.space_order, steps, vectorize=vec)
+    other = None
+    if not args.cpu_single_build:
+        v2, _, s2 = cpu_oracle(n, args.space_order, steps, vectorize=not vec)
+        other = {'value': v2, 'flags': cpu_flags(not vec), 'seconds': s2}
+    base = {'value': val, 'unit': UNIT, 'cores': cores, 'kind': 'port', 'cpu_model': cpu_model(),
+            'omp_proc_bind': 'close',
+            'sample': '%d steps of the %d^3 problem, reference-shaped generated C++ (g++ %s), time loop only'
+                      % (steps, n, cpu_flags(vec))}
+    if other:
+        base['reference_flags' if vec else 'vectorized'] = other
     line = {
         'impl': 'reference', 'metric': METRIC, 'value': val, 'unit': UNIT,
         'n_gpus': args.gpus, 'steps': steps, 'warmup': 0, 'ms_per_step': secs * 1e3 / steps,
-        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
+        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': args.storage,
         'data': 'synthetic (seeded layered medium, Ricker source)',
-        'config': {'workload': 'elastic %d^3 SO%d FP32 heterogeneous + Ricker source, free surfaces' % (n, args.space_order),
-                   'grid': [n, n, n], 'space_order': args.space_order, 'l2_flush': 'inputs larger than L2'},
-        'cpu_baseline': {'value': val, 'unit': UNIT, 'cores': cores, 'kind': 'port',
-                         'sample': '%d steps of the %d^3 problem, reference-shaped generated C++ '
-                                   '(g++ %s), time loop only' % (steps, n, cpu_flags(args.cpu_vectorize))},
+        'config': elastic_config(args.size, args.space_order, args.storage, args.gpus, args.variant),
+        'cpu_baseline': base,
         'e2e': {'value': val, 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
     }
     print(json.dumps(line), flush=True)
@@ -326,9 +379,13 @@ def main():
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--scheme', default='elastic', choices=['elastic', 'acoustic'])
-    # reference arm only: g++ -O3 -fopenmp with vectorisation on instead of
-    # the reference's own -fno-tree-vectorize build flags
-    ap.add_argument('--cpu-vectorize', action='store_true')
+    # reference arm: the stated value is the g++ -O3 -fopenmp build (the
+    # reference's generated C++ as "g++ -O3, OpenMP"); --cpu-reference-flags
+    # states the reference's own -fno-tree-vectorize build instead, and
+    # --cpu-single-build skips timing the other build beside it
+    ap.add_argument('--cpu-reference-flags', action='store_true')
+    ap.add_argument('--cpu-single-build', action='store_true')
+    ap.add_argument('--cpu-vectorize', action='store_true', help=argparse.SUPPRESS)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()
@@ -422,12 +479,10 @@ def main():
         t0 = time.perf_counter()
         sim.zero()
         sim.steps = 0
-        sim.set_media(*host_media)
+        sim.set_media_async(*host_media)
         sim.set_source(src, wav)
         sim.step(args.steps)
-        lvl = args.steps % 2
-        for i in range(9):
-            sim.lib.ofd_download_field(sim.h, i, lvl, host_fields[i].ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+        sim.download_all_async(host_fields, level=args.steps % 2)
         sim.sync()
         wall = time.perf_counter() - t0
         cells = float(np.prod(sim.dims))
@@ -441,11 +496,7 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
-            v, cores, secs = cpu_oracle(args.cpu_size, so, args.cpu_steps)
-            cpu = {'value': v, 'unit': UNIT, 'cores': cores, 'kind': 'port',
-                   'sample': '%d steps of a %d^3 problem of the same kind (SO%d, heterogeneous, source), '
-                             'reference-shaped generated C++ (g++ -g -O3 -fno-tree-vectorize -fopenmp), '
-                             'time loop only, %.1f s' % (args.cpu_steps, args.cpu_size, so, secs)}
+            cpu = cpu_baseline_pair(args.cpu_size, so, args.cpu_steps)
         except Exception as e:  # report, do not hide
             cpu = {'value': None, 'error': str(e)[:300]}
 
@@ -455,10 +506,8 @@ def main():
             'warmup': args.warmup, 'ms_per_step': ms / args.steps, 'higher_is_better': True,
             'scaling': 'weak', 'vs_baseline': None, 'dtype': args.storage,
             'data': 'synthetic (seeded layered medium, Ricker source)',
-            'config': {'workload': 'elastic %d^3 SO%d %s heterogeneous + Ricker source, free surfaces' % (n, so, args.storage.upper()),
-                       'grid': [n, n, n], 'space_order': so, 'parallelism': 'replicas x%d' % world,
-                       'l2_flush': 'inputs larger than L2 (%.1f GB resident)' % (runtime.Simulation.footprint(cfg) / 1e9),
-                       'kernel_variant': args.variant},
+            'config': elastic_config(n, so, args.storage, world, args.variant),
+            'l2_flush_detail': 'inputs larger than L2: %.1f GB resident' % (runtime.Simulation.footprint(cfg) / 1e9),
             'roofline': roofline, 'cpu_baseline': cpu, 'e2e': e2e, 'clocks': clocks,
             'gpu_launches': launches,
         }

@@ -83,6 +83,11 @@ int ofd_footprint(const ofd_config *cfg, size_t *bytes);
  * staggeredgrid.py:571-597 are computed on the device. */
 int ofd_set_media_const(ofd_handle *h, float beta, float lambda, float mu);
 int ofd_set_media(ofd_handle *h, const float *rho, const float *vp, const float *vs);
+/* ofd_set_media queued on the handle's stream without waiting (no
+ * counterpart in the reference): the arrays (host or device memory) must stay
+ * valid until the stream reaches the copy; pinned host memory makes the copy
+ * asynchronous.  ofd_sync waits for it. */
+int ofd_set_media_async(ofd_handle *h, const float *rho, const float *vp, const float *vs);
 
 /* Literal tables of the generated update expressions (required before
  * ofd_step).  The sweeps evaluate the reference generator's expanded,
@@ -95,9 +100,18 @@ int ofd_set_media(ofd_handle *h, const float *rho, const float *vp, const float 
  * sizes of the prebuilt expression for this space order and media mode. */
 int ofd_set_coefficients(ofd_handle *h, int het, const float *ks, int nks, const float *kv, int nkv);
 
-/* Field transfer, reference layout, host memory (pageable or pinned). */
+/* Field transfer, reference layout, host memory (pageable or pinned); the
+ * calls return once the copy is complete.  The reference publishes its host
+ * arrays through OpesciGrid after opesci_execute (regulargrid.py:445-464),
+ * which the generated program's opesci_execute does with these calls. */
 int ofd_upload_field(ofd_handle *h, int field, int level, const float *host);
 int ofd_download_field(ofd_handle *h, int field, int level, float *host);
+/* The same queued on the handle's stream without waiting (no counterpart in
+ * the reference): several fields' copies then run back to back, and with
+ * pinned host memory they overlap other host work.  The host array must stay
+ * valid (and, for downloads, unread) until ofd_sync returns. */
+int ofd_upload_field_async(ofd_handle *h, int field, int level, const float *host);
+int ofd_download_field_async(ofd_handle *h, int field, int level, float *host);
 /* Same with device memory in the reference layout. */
 int ofd_upload_field_device(ofd_handle *h, int field, int level, const float *dev);
 int ofd_download_field_device(ofd_handle *h, int field, int level, float *dev);
@@ -158,6 +172,14 @@ int ofd_step_graph(ofd_handle *h, int nsteps);
  * 1..64), plain-kernel block shape (bx multiple of 32, bx*by <= 256). */
 int ofd_set_tuning(ofd_handle *h, int stress_variant, int velocity_variant, int chunk_waves, int plain_bx,
                    int plain_by);
+/* Limit of every device-side wait of the handle's kernels (no counterpart in
+ * the reference, whose OpenMP loop has no device waits): the TMA pipeline
+ * waits of the tiled sweeps and the grid barriers of persistent stepping.
+ * A wait that runs out sets the handle's error word, its kernel drains the
+ * copies it has in flight and returns, and the next ofd_sync (or timed or
+ * profiled step) reports OFD_ETIMEOUT; the context stays usable.  Default
+ * 10 s; seconds in (0, 600].  Cached graphs are rebuilt. */
+int ofd_set_wait_limit(ofd_handle *h, double seconds);
 /* Persistent time stepping (no counterpart in the reference): when enabled,
  * ofd_step and ofd_step_graph run up to 1024 whole steps per cooperative
  * launch, with grid barriers between the phases of a step.  For small grids,
@@ -227,10 +249,13 @@ int ofd_field_view_get(ofd_handle *h, int field, int level, ofd_field_view *out)
  * [margin, dims-margin)^3; *out (device memory) receives the sum.  Work is
  * queued on stream (a cudaStream_t, NULL for the default stream).  Partial
  * sums live in a fixed 32 KB device array of the library, one entry per x
- * plane: at most 4096 interior planes, larger grids are rejected.  The first
- * call on each device looks up that array's device address; make it before
- * any stream capture.  All calls share the array: calls whose work overlaps
- * on the GPU race and must be serialised.  ofd_noalloc_last_error() describes
+ * plane: at most 4096 interior planes (and at most 2^31 - 1 interior points
+ * per plane), larger grids are rejected.  A call outside stream capture looks
+ * up that array's device address in the current CUDA context and records it;
+ * a call on a capturing stream uses the recorded address, so the first call
+ * in each context (again after cudaDeviceReset) must come before any stream
+ * capture.  All calls share the array: calls whose work overlaps on the GPU
+ * race and must be serialised.  ofd_noalloc_last_error() describes
  * the last failure of this entry point on the calling thread. */
 int ofd_sumsq_field_noalloc(const float *field, const int dims[3], int margin, double *out, void *stream);
 const char *ofd_noalloc_last_error(void);

@@ -70,6 +70,7 @@ template <typename S> struct SweepArgs {
   typename Storage<S>::C dt, ih1, ih2, ih3;
   typename Storage<S>::C c[4];
   int xchunk;          // planes per CTA along x
+  float nz;            // -0.0f: the addend that keeps paired products unfused (ofd_f32x2.cuh)
   float K[OFD_MAX_K];  // literal table of the generated update expression
 };
 

@@ -88,6 +88,8 @@ struct Backend {
   virtual void group_step(GroupPlanBase *plan, int t0, cudaStream_t st) = 0;
   // the handle's sweeps can run tiled (a group member must)
   virtual bool tiled_ok(const DevState &s) const = 0;
+  // the handle's literal table of a sweep repeats its values as KMap says
+  virtual bool kmap_ok(const DevState &s, bool stress) const = 0;
 };
 
 Backend *make_backend_f32(int R);
@@ -225,6 +227,7 @@ struct Impl : Backend {
     a.ih3 = (C)(1.0 / s.h[2]);
     for (int k = 0; k < 4; ++k) a.c[k] = (C)s.c[k];
     a.xchunk = 0;
+    a.nz = -0.0f;
     const float *K = stress ? s.Ks : s.Kv;
     const int nk = stress ? s.nks : s.nkv;
     for (int k = 0; k < OFD_MAX_K; ++k) a.K[k] = k < nk ? K[k] : 0.f;
@@ -400,6 +403,7 @@ struct Impl : Backend {
     a.ssc[2] = s.scale[F_TZZ];
     a.bar = s.d_bar;
     a.err = s.tiled.err;
+    a.wait_ns = s.tiled.wait_ns;
     for (int p = 0; p < 2; ++p) a.rec[p] = rec_args(s, 1 - p);
     a.nsteps = nsteps;
     a.p0 = p0;
@@ -612,6 +616,11 @@ struct Impl : Backend {
   }
 
   bool tiled_ok(const DevState &s) const override { return s.tiled.maps && tiled_supported<R, S>(s.g); }
+
+  bool kmap_ok(const DevState &s, bool stress) const override {
+    const DevState *m[1] = {&s};
+    return stress ? tables_follow_kmap<true>(m, 1) : tables_follow_kmap<false>(m, 1);
+  }
 
   int table_size(int het, int stress) const override {
     if (het) return stress ? GenSweep<R, 1>::NK_STRESS : GenSweep<R, 1>::NK_VELOCITY;

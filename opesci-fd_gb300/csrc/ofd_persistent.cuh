@@ -43,6 +43,7 @@ struct PersistArgs {
   float ssc[3];         // storage scales of Txx Tyy Tzz
   unsigned *bar;        // [0] arrivals, [1] generation
   int *err;
+  unsigned long long wait_ns;   // limit of each grid-barrier wait (handle setting)
   int nsteps;
   int p0;               // parity of the first step
   RecArgs<S> rec[2];    // receivers by parity of t0 (level t1 = 1 - p)
@@ -54,8 +55,10 @@ __device__ __forceinline__ unsigned long long wall_ns() {
   return t;
 }
 
-// Bounded grid barrier; false when it (or another block's) wait expired.
-__device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err) {
+// Bounded grid barrier; false when its wait (limit_ns of %globaltimer) or
+// another block's expired.  A waiting block also leaves as soon as another
+// block has set the error word, so one expiry ends every block's wait.
+__device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err, unsigned long long limit_ns) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -72,7 +75,11 @@ __device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err) {
       const unsigned long long t0 = wall_ns();
       while (*gen == g) {
         __nanosleep(32);
-        if (wall_ns() - t0 > 10000000000ULL) {
+        if (*(volatile int *)err) {
+          ok = 0;
+          break;
+        }
+        if (wall_ns() - t0 > limit_ns) {
           atomicExch(err, 3);
           ok = 0;
           break;
@@ -113,7 +120,7 @@ __global__ void __launch_bounds__(256) persistent_steps_kernel(const __grid_cons
         for (int f = 0; f < 6; ++f) sa.out[F_TXX + f][o] = Storage<S>::store(out[f], sa.sc[F_TXX + f]);
       }
     }
-    if (!grid_barrier(a.bar, a.err)) return;
+    if (!grid_barrier(a.bar, a.err, a.wait_ns)) return;
     // stress ghosts, one phase per face normal
     for (int d = 0; d < 3; ++d) {
       int a1, a2;
@@ -127,7 +134,7 @@ __global__ void __launch_bounds__(256) persistent_steps_kernel(const __grid_cons
         const int zz = (int)(r / n1);
         stress_bc_point<R, S, true>(a.sbc[p], d, i1, i2, zz >> 1, zz & 1);
       }
-      if (!grid_barrier(a.bar, a.err)) return;
+      if (!grid_barrier(a.bar, a.err, a.wait_ns)) return;
     }
     // velocity sweep
     {
@@ -145,7 +152,7 @@ __global__ void __launch_bounds__(256) persistent_steps_kernel(const __grid_cons
         for (int f = 0; f < 3; ++f) va.out[F_U + f][o] = Storage<S>::store(out[f], va.sc[F_U + f]);
       }
     }
-    if (!grid_barrier(a.bar, a.err)) return;
+    if (!grid_barrier(a.bar, a.err, a.wait_ns)) return;
     // velocity ghosts, one phase per face normal; the source and the step
     // counter ride on the first
     for (int d = 0; d < 3; ++d) {
@@ -169,7 +176,7 @@ __global__ void __launch_bounds__(256) persistent_steps_kernel(const __grid_cons
         }
         *a.d_step = st + 1;
       }
-      if (!grid_barrier(a.bar, a.err)) return;
+      if (!grid_barrier(a.bar, a.err, a.wait_ns)) return;
     }
     // receivers read level t1, which the next step's phases do not write
     // (they write the other level), so no barrier follows

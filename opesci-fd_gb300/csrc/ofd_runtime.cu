@@ -40,43 +40,53 @@ int fail_msg(int code, const char *msg) { return fail(code, "%s", msg); }
 
 // Media preprocessing (staggeredgrid.py:571-597), evaluated in double and
 // rounded to float like the reference's C expressions, on the whole padded
-// grid with upper neighbours clamped at the last index.
-__global__ void media_base_kernel(const float *rho, const float *vp, const float *vs, float *beta,
-                                  float *lam, float *mu, double *inv_mu, long n) {
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-    const double r = rho[i], p = vp[i], s = vs[i];
-    beta[i] = (float)(1.0 / r);
-    lam[i] = (float)(r * (p * p - 2.0 * (s * s)));
-    const float m = (float)(r * (s * s));
-    mu[i] = m;
-    inv_mu[i] = 1.0 / (double)m;   // the 1.0/mu of the harmonic means, computed once per point
-  }
+// grid with upper neighbours clamped at the last index: beta = 1/rho,
+// lambda = rho (vp^2 - 2 vs^2), mu = rho vs^2; beta1..3 the means of beta and
+// its upper neighbour along x/y/z; mu12/13/23 the harmonic means of mu over
+// the four points of the cell edge (1/mu in double).  One pass: beta, lambda,
+// mu and 1/mu are recomputed at the upper neighbours from rho, vp, vs rather
+// than read back from intermediate arrays.  Thread (z, y) of block row (y, x)
+// handles one point; no index divisions.
+__device__ __forceinline__ void media_point(const float *rho, const float *vp, const float *vs, long i, float *beta,
+                                            float *lam, float *mu, double *inv_mu) {
+  const double r = rho[i], p = vp[i], s = vs[i];
+  *beta = (float)(1.0 / r);
+  *lam = (float)(r * (p * p - 2.0 * (s * s)));
+  const float m = (float)(r * (s * s));
+  *mu = m;
+  *inv_mu = 1.0 / (double)m;
 }
 
-__global__ void media_avg_kernel(const float *beta, const float *lam, const float *mu, const double *im, Geom g,
-                                 float *o_lam, float *o_mu, float *o_mu12, float *o_mu13,
-                                 float *o_mu23, float *o_b1, float *o_b2, float *o_b3, float *o_beta) {
-  const long n = (long)g.n1 * g.n2 * g.n3;
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-    const int z = (int)(i % g.n3);
-    const long r = i / g.n3;
-    const int y = (int)(r % g.n2);
-    const int x = (int)(r / g.n2);
-    const int x1 = x + 1 < g.n1 ? x + 1 : x, y1 = y + 1 < g.n2 ? y + 1 : y, z1 = z + 1 < g.n3 ? z + 1 : z;
-    auto D = [&](int a, int b, int c) { return ((long)a * g.n2 + b) * g.n3 + c; };
-    const long o = (long)x * g.plane + (long)y * g.P + z;
-    o_lam[o] = lam[i];
-    o_mu[o] = mu[i];
-    const float b0 = beta[i];
-    o_beta[o] = b0;
-    o_b1[o] = (b0 + beta[D(x1, y, z)]) * 0.5f;
-    o_b2[o] = (b0 + beta[D(x, y1, z)]) * 0.5f;
-    o_b3[o] = (b0 + beta[D(x, y, z1)]) * 0.5f;
-    const double m0 = im[i];
-    o_mu12[o] = (float)(1.0 / (0.25 * (m0 + im[D(x1, y, z)] + im[D(x, y1, z)] + im[D(x1, y1, z)])));
-    o_mu13[o] = (float)(1.0 / (0.25 * (m0 + im[D(x1, y, z)] + im[D(x, y, z1)] + im[D(x1, y, z1)])));
-    o_mu23[o] = (float)(1.0 / (0.25 * (m0 + im[D(x, y1, z)] + im[D(x, y, z1)] + im[D(x, y1, z1)])));
-  }
+__global__ void media_fused_kernel(const float *__restrict__ rho, const float *__restrict__ vp,
+                                   const float *__restrict__ vs, Geom g, float *o_lam, float *o_mu, float *o_mu12,
+                                   float *o_mu13, float *o_mu23, float *o_b1, float *o_b2, float *o_b3,
+                                   float *o_beta) {
+  const int z = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int x = blockIdx.z;
+  if (z >= g.n3 || y >= g.n2) return;
+  const int x1 = x + 1 < g.n1 ? x + 1 : x, y1 = y + 1 < g.n2 ? y + 1 : y, z1 = z + 1 < g.n3 ? z + 1 : z;
+  auto D = [&](int a, int b, int c) { return ((long)a * g.n2 + b) * g.n3 + c; };
+  float b0, l0, m0f, bx, by, bz, lt, mt;
+  double im0, imx, imy, imz, imxy, imxz, imyz;
+  media_point(rho, vp, vs, D(x, y, z), &b0, &l0, &m0f, &im0);
+  media_point(rho, vp, vs, D(x1, y, z), &bx, &lt, &mt, &imx);
+  media_point(rho, vp, vs, D(x, y1, z), &by, &lt, &mt, &imy);
+  media_point(rho, vp, vs, D(x, y, z1), &bz, &lt, &mt, &imz);
+  float bt;
+  media_point(rho, vp, vs, D(x1, y1, z), &bt, &lt, &mt, &imxy);
+  media_point(rho, vp, vs, D(x1, y, z1), &bt, &lt, &mt, &imxz);
+  media_point(rho, vp, vs, D(x, y1, z1), &bt, &lt, &mt, &imyz);
+  const long o = (long)x * g.plane + (long)y * g.P + z;
+  o_lam[o] = l0;
+  o_mu[o] = m0f;
+  o_beta[o] = b0;
+  o_b1[o] = (b0 + bx) * 0.5f;
+  o_b2[o] = (b0 + by) * 0.5f;
+  o_b3[o] = (b0 + bz) * 0.5f;
+  o_mu12[o] = (float)(1.0 / (0.25 * (im0 + imx + imy + imxy)));
+  o_mu13[o] = (float)(1.0 / (0.25 * (im0 + imx + imz + imxz)));
+  o_mu23[o] = (float)(1.0 / (0.25 * (im0 + imy + imz + imyz)));
 }
 
 __global__ void fill_kernel(float *p, long n, float v) {
@@ -371,6 +381,8 @@ int ofd_create(const ofd_config *cfg, ofd_handle **out) {
   h->s.tiled.err = h->d_err;
   h->s.tiled.z0 = L.z0;
   h->s.tiled.waves = 1;
+  h->s.tiled.kd[0] = h->s.tiled.kd[1] = 0;
+  h->s.tiled.wait_ns = 10000000000ULL;
   if (!encode_fn()) {
     ofd_destroy(h);
     return fail(OFD_ECUDA, "the driver does not provide cuTensorMapEncodeTiled");
@@ -416,6 +428,8 @@ int ofd_set_coefficients(ofd_handle *h, int het, const float *ks, int nks, const
   h->s.nkv = nkv;
   for (int i = 0; i < nks; ++i) h->s.Ks[i] = ks[i];
   for (int i = 0; i < nkv; ++i) h->s.Kv[i] = kv[i];
+  h->s.tiled.kd[1] = het && h->be->kmap_ok(h->s, true) ? 1 : 0;
+  h->s.tiled.kd[0] = het && h->be->kmap_ok(h->s, false) ? 1 : 0;
   h->be->prepare(h->s);
   drop_graphs(h);
   OFD_CUDA(cudaGetLastError());
@@ -433,27 +447,38 @@ int ofd_set_media_const(ofd_handle *h, float beta, float lambda, float mu) {
   return OFD_OK;
 }
 
-int ofd_set_media(ofd_handle *h, const float *rho, const float *vp, const float *vs) {
-  if (!h || !rho || !vp || !vs) return fail(OFD_EINVAL, "null argument");
+// Queue the media preprocessing on the handle's stream: rho, vp, vs (host or
+// device memory, dense reference layout) in, the nine effective-media arrays
+// out.  The three inputs pass through one stream-ordered scratch allocation.
+static int queue_media(ofd_handle *h, const float *rho, const float *vp, const float *vs, cudaMemcpyKind kind) {
   const Geom &g = h->s.g;
   const long n = (long)g.n1 * g.n2 * g.n3;
   float *tmp = nullptr;
-  // six float arrays then one double array
-  OFD_CUDA(cudaMallocAsync((void **)&tmp, sizeof(float) * n * 6 + sizeof(double) * n + 256, h->stream));
-  double *inv_mu = (double *)(((uintptr_t)(tmp + 6 * n) + 255) & ~(uintptr_t)255);
-  OFD_CUDA(cudaMemcpyAsync(tmp, rho, sizeof(float) * n, cudaMemcpyHostToDevice, h->stream));
-  OFD_CUDA(cudaMemcpyAsync(tmp + n, vp, sizeof(float) * n, cudaMemcpyHostToDevice, h->stream));
-  OFD_CUDA(cudaMemcpyAsync(tmp + 2 * n, vs, sizeof(float) * n, cudaMemcpyHostToDevice, h->stream));
-  media_base_kernel<<<1216, 256, 0, h->stream>>>(tmp, tmp + n, tmp + 2 * n, tmp + 3 * n, tmp + 4 * n, tmp + 5 * n,
-                                                 inv_mu, n);
-  media_avg_kernel<<<1216, 256, 0, h->stream>>>(tmp + 3 * n, tmp + 4 * n, tmp + 5 * n, inv_mu, g, h->s.media[M_LAM],
-                                                h->s.media[M_MU], h->s.media[M_MU12], h->s.media[M_MU13],
-                                                h->s.media[M_MU23], h->s.media[M_B1], h->s.media[M_B2],
-                                                h->s.media[M_B3], h->s.media[M_BETA]);
+  OFD_CUDA(cudaMallocAsync((void **)&tmp, sizeof(float) * n * 3, h->stream));
+  OFD_CUDA(cudaMemcpyAsync(tmp, rho, sizeof(float) * n, kind, h->stream));
+  OFD_CUDA(cudaMemcpyAsync(tmp + n, vp, sizeof(float) * n, kind, h->stream));
+  OFD_CUDA(cudaMemcpyAsync(tmp + 2 * n, vs, sizeof(float) * n, kind, h->stream));
+  const dim3 blk(32, 8), grd((g.n3 + 31) / 32, (g.n2 + 7) / 8, g.n1);
+  media_fused_kernel<<<grd, blk, 0, h->stream>>>(tmp, tmp + n, tmp + 2 * n, g, h->s.media[M_LAM], h->s.media[M_MU],
+                                                 h->s.media[M_MU12], h->s.media[M_MU13], h->s.media[M_MU23],
+                                                 h->s.media[M_B1], h->s.media[M_B2], h->s.media[M_B3],
+                                                 h->s.media[M_BETA]);
   OFD_CUDA(cudaGetLastError());
   OFD_CUDA(cudaFreeAsync(tmp, h->stream));
+  return OFD_OK;
+}
+
+int ofd_set_media(ofd_handle *h, const float *rho, const float *vp, const float *vs) {
+  if (!h || !rho || !vp || !vs) return fail(OFD_EINVAL, "null argument");
+  const int rc = queue_media(h, rho, vp, vs, cudaMemcpyDefault);
+  if (rc) return rc;
   OFD_CUDA(cudaStreamSynchronize(h->stream));
   return OFD_OK;
+}
+
+int ofd_set_media_async(ofd_handle *h, const float *rho, const float *vp, const float *vs) {
+  if (!h || !rho || !vp || !vs) return fail(OFD_EINVAL, "null argument");
+  return queue_media(h, rho, vp, vs, cudaMemcpyDefault);
 }
 
 static int check_fl(ofd_handle *h, int field, int level) {
@@ -479,17 +504,52 @@ int ofd_download_field_device(ofd_handle *h, int field, int level, float *dev) {
   return OFD_OK;
 }
 
-int ofd_upload_field(ofd_handle *h, int field, int level, const float *host) {
-  int rc = check_fl(h, field, level);
-  if (rc) return rc;
+// Host <-> device field transfers in stream order.  FP32 storage copies the
+// padded rows straight to/from the dense host array (one pitched copy: rows of
+// dim3 floats at the padded pitch); other storage types convert through a
+// stream-ordered dense FP32 scratch array.
+static int queue_upload(ofd_handle *h, int field, int level, const float *host) {
   const Geom &g = h->s.g;
+  if (h->s.storage == OFD_F32) {
+    float *dst = (float *)h->s.field[field] + (size_t)level * g.level;
+    OFD_CUDA(cudaMemcpy2DAsync(dst, sizeof(float) * g.P, host, sizeof(float) * g.n3, sizeof(float) * g.n3,
+                               (size_t)g.n1 * g.n2, cudaMemcpyDefault, h->stream));
+    return OFD_OK;
+  }
   const long n = (long)g.n1 * g.n2 * g.n3;
   float *tmp = nullptr;
   OFD_CUDA(cudaMallocAsync((void **)&tmp, sizeof(float) * n, h->stream));
-  OFD_CUDA(cudaMemcpyAsync(tmp, host, sizeof(float) * n, cudaMemcpyHostToDevice, h->stream));
+  OFD_CUDA(cudaMemcpyAsync(tmp, host, sizeof(float) * n, cudaMemcpyDefault, h->stream));
   h->be->to_padded(h->s, tmp, field, level, h->stream);
   OFD_CUDA(cudaGetLastError());
   OFD_CUDA(cudaFreeAsync(tmp, h->stream));
+  return OFD_OK;
+}
+
+static int queue_download(ofd_handle *h, int field, int level, float *host) {
+  const Geom &g = h->s.g;
+  if (h->s.storage == OFD_F32) {
+    const float *src = (const float *)h->s.field[field] + (size_t)level * g.level;
+    OFD_CUDA(cudaMemcpy2DAsync(host, sizeof(float) * g.n3, src, sizeof(float) * g.P, sizeof(float) * g.n3,
+                               (size_t)g.n1 * g.n2, cudaMemcpyDefault, h->stream));
+    return OFD_OK;
+  }
+  const long n = (long)g.n1 * g.n2 * g.n3;
+  float *tmp = nullptr;
+  OFD_CUDA(cudaMallocAsync((void **)&tmp, sizeof(float) * n, h->stream));
+  h->be->from_padded(h->s, tmp, field, level, h->stream);
+  OFD_CUDA(cudaGetLastError());
+  OFD_CUDA(cudaMemcpyAsync(host, tmp, sizeof(float) * n, cudaMemcpyDefault, h->stream));
+  OFD_CUDA(cudaFreeAsync(tmp, h->stream));
+  return OFD_OK;
+}
+
+int ofd_upload_field(ofd_handle *h, int field, int level, const float *host) {
+  int rc = check_fl(h, field, level);
+  if (rc) return rc;
+  if (!host) return fail(OFD_EINVAL, "null host array");
+  rc = queue_upload(h, field, level, host);
+  if (rc) return rc;
   OFD_CUDA(cudaStreamSynchronize(h->stream));
   return OFD_OK;
 }
@@ -497,16 +557,25 @@ int ofd_upload_field(ofd_handle *h, int field, int level, const float *host) {
 int ofd_download_field(ofd_handle *h, int field, int level, float *host) {
   int rc = check_fl(h, field, level);
   if (rc) return rc;
-  const Geom &g = h->s.g;
-  const long n = (long)g.n1 * g.n2 * g.n3;
-  float *tmp = nullptr;
-  OFD_CUDA(cudaMallocAsync((void **)&tmp, sizeof(float) * n, h->stream));
-  h->be->from_padded(h->s, tmp, field, level, h->stream);
-  OFD_CUDA(cudaGetLastError());
-  OFD_CUDA(cudaMemcpyAsync(host, tmp, sizeof(float) * n, cudaMemcpyDeviceToHost, h->stream));
-  OFD_CUDA(cudaFreeAsync(tmp, h->stream));
+  if (!host) return fail(OFD_EINVAL, "null host array");
+  rc = queue_download(h, field, level, host);
+  if (rc) return rc;
   OFD_CUDA(cudaStreamSynchronize(h->stream));
   return OFD_OK;
+}
+
+int ofd_upload_field_async(ofd_handle *h, int field, int level, const float *host) {
+  int rc = check_fl(h, field, level);
+  if (rc) return rc;
+  if (!host) return fail(OFD_EINVAL, "null host array");
+  return queue_upload(h, field, level, host);
+}
+
+int ofd_download_field_async(ofd_handle *h, int field, int level, float *host) {
+  int rc = check_fl(h, field, level);
+  if (rc) return rc;
+  if (!host) return fail(OFD_EINVAL, "null host array");
+  return queue_download(h, field, level, host);
 }
 
 int ofd_zero_fields(ofd_handle *h) {
@@ -653,7 +722,8 @@ static int check_err_word(ofd_handle *h) {
   if (err) {
     cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream);
     cudaStreamSynchronize(h->stream);
-    return fail(OFD_ETIMEOUT, "a bounded device wait expired in a tiled sweep (error word %d)", err);
+    return fail(OFD_ETIMEOUT, "a bounded device wait expired (error word %d: %s)", err,
+                err == 3 ? "grid barrier of the persistent kernel" : "pipeline wait of a tiled sweep");
   }
   return OFD_OK;
 }
@@ -702,6 +772,15 @@ int ofd_set_tuning(ofd_handle *h, int stress_variant, int velocity_variant, int 
   h->s.tiled.waves = chunk_waves;
   h->s.plain_bx = plain_bx;
   h->s.plain_by = plain_by;
+  drop_graphs(h);
+  return OFD_OK;
+}
+
+int ofd_set_wait_limit(ofd_handle *h, double seconds) {
+  if (!h) return fail(OFD_EINVAL, "null handle");
+  if (!(seconds > 0) || seconds > 600) return fail(OFD_EINVAL, "wait limit must be in (0, 600] seconds");
+  h->s.tiled.wait_ns = (unsigned long long)(seconds * 1e9);
+  if (h->s.tiled.wait_ns == 0) h->s.tiled.wait_ns = 1;
   drop_graphs(h);
   return OFD_OK;
 }

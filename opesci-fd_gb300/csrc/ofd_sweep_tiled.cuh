@@ -25,6 +25,7 @@
 #include <cuda.h>
 #include "ofd_common.cuh"
 #include "generated/sweeps_gen.cuh"
+#include "ofd_f32x2.cuh"
 
 namespace ofd {
 
@@ -55,6 +56,8 @@ struct TiledCtx {
   int *err;              // device error word
   int z0;                // element offset of z = 0 in a padded row
   int waves;             // CTA-count multiplier (autotuner knob), 1 = default
+  int kd[2];             // [stress]: the literal table follows KMap (register-held literals)
+  unsigned long long wait_ns;   // limit of each pipeline wait
 };
 
 // Box extents the runtime encodes into the descriptors.
@@ -77,6 +80,7 @@ struct TiledParams {
   CUtensorMap mmap[5];     // point boxes of media arrays
   CUtensorMap bmap;        // beta boxes (heterogeneous velocity sweep)
   int *err;                // error word (bounded waits)
+  unsigned long long wait_ns;   // limit of each pipeline wait (ns of %globaltimer)
   int zcoord0;             // TMA x coordinate of z = m (z0 + m)
   int chunk;               // planes per CTA along x
   int ntz, nty;            // tiles along z, y
@@ -109,7 +113,8 @@ __device__ __forceinline__ unsigned long long global_ns() {
 }
 
 // Bounded wait; false when 10 s of wall time ran out (a time bound, not an
-// iteration count, so heavy concurrent load never trips it spuriously).
+// iteration count, so heavy concurrent load never trips it spuriously).  Used
+// by the drain after an abort, which waits for copies already in flight.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
   if (mbar_try_wait(bar, parity)) return true;
   const unsigned long long t0 = global_ns();
@@ -120,16 +125,18 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
   }
 }
 
-// Bounded wait that also returns false once another warp of the CTA has
-// aborted (*abort != 0).
-__device__ __forceinline__ bool mbar_wait_or_abort(uint64_t *bar, unsigned parity, volatile int *abort) {
+// Bounded wait of the pipeline (limit_ns of wall time, the handle's wait
+// limit) that also returns false once another warp of the CTA has aborted
+// (*abort != 0).
+__device__ __forceinline__ bool mbar_wait_or_abort(uint64_t *bar, unsigned parity, volatile int *abort,
+                                                   unsigned long long limit_ns) {
   if (mbar_try_wait(bar, parity)) return true;
   const unsigned long long t0 = global_ns();
   for (;;) {
     for (int i = 0; i < 64; ++i)
       if (mbar_try_wait(bar, parity)) return true;
     if (*abort) return false;
-    if (global_ns() - t0 > 10000000000ULL) return false;
+    if (global_ns() - t0 > limit_ns) return false;
   }
 }
 
@@ -146,6 +153,14 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, u
 
 __host__ __device__ constexpr int round128(int b) { return (b + 127) / 128 * 128; }
 
+// Paired evaluation (ofd_f32x2.cuh): heterogeneous media and FP32 arithmetic
+// (FP32, FP16 or BF16 storage).  Each consumer lane then owns two adjacent z
+// points and one warp covers a 64-point tile row.  The literal table is then
+// passed as pairs {K, K} (KRegs2 or KPairPtr below).
+template <typename S, int HET> struct PairMode {
+  static constexpr bool v = HET != 0 && sizeof(S) <= 4;
+};
+
 // Compile-time description of one sweep.  Roles of the arrays read:
 //   X  ("x-window"): read at x offsets and with y/z neighbours -> ring of NSH
 //      halo boxes (stress: U V W; velocity: Txx Txy Txz)
@@ -155,8 +170,9 @@ __host__ __device__ constexpr int round128(int b) { return (b + 127) / 128 * 128
 //      velocity: U V W at t0) and the media arrays -> ring of NSC point boxes
 template <int R, typename S, int HET, bool STRESS>
 struct TiledCfg {
+  static constexpr bool PAIR = PairMode<S, HET>::v;
   static constexpr int TY = tile_rows(R);
-  static constexpr int ZW = row_warps(R);                  // consumer warps per tile row
+  static constexpr int ZW = PAIR ? 1 : row_warps(R);       // consumer warps per tile row
   static constexpr int NCW = TY * ZW;                      // consumer warps
   static constexpr int THREADS = 32 * (NCW + 1);           // + one producer warp
   static constexpr int ZH = ZHalo<S>::v;                  // z halo, rounded to 16 B
@@ -237,7 +253,7 @@ struct TiledAcc {
   }
   __device__ __forceinline__ C m(int i) const {
     if constexpr (G::NBX != 0) {
-      // beta1..3 = (beta + beta at x+1 / y+1 / z+1) * 0.5f, as media_avg_kernel
+      // beta1..3 = (beta + beta at x+1 / y+1 / z+1) * 0.5f, as media_fused_kernel
       const float *b = (const float *)(xs[R] + G::NXF * G::HSLOT);
       const float b0 = b[bpos];
       float b1;
@@ -251,11 +267,61 @@ struct TiledAcc {
   }
 };
 
-template <int R> struct TiledThreads { static constexpr int v = 32 * (tile_rows(R) * row_warps(R) + 1); };
-// resident CTAs per SM the register budget is sized for: space order >= 6
-// keeps one CTA per SM (its rings fill shared memory), so tell ptxas it may
-// use the whole register file rather than spill
-template <int R> struct TiledMinBlocks { static constexpr int v = R >= 3 ? 1 : 0; };
+// Accessor of the paired evaluation: the same reads as TiledAcc for the two
+// points (z, z + 1) of the thread, as one register pair.  hpos, ppos and bpos
+// are even, so a read at an even z offset is one vector load of both values
+// and a read at an odd offset two scalar loads.
+template <int R, typename S, int HET, bool STRESS>
+struct TiledAcc2 {
+  typedef TiledCfg<R, S, HET, STRESS> G;
+  const unsigned char *xs[2 * R + 1];
+  const unsigned char *cs;
+  const float *inv;
+  F2 nz;   // -0.0 pair from a kernel argument (see ofd_f32x2.cuh)
+  int hpos, ppos, bpos;
+  __device__ __forceinline__ F2 operator()(int f, int dx, int dy, int dz) const {
+    const S *b;
+    int pos;
+    if (G::role(f) == 0) {
+      b = (const S *)(xs[dx + R] + G::xidx(f) * G::HSLOT);
+      pos = hpos + dy * G::HW + dz;
+    } else if (G::role(f) == 1) {
+      b = (const S *)(cs + G::h0off(G::h0idx(f)));
+      pos = hpos + dy * G::HW + dz;
+    } else {
+      b = (const S *)(cs + G::poff(G::pidx(f)));
+      pos = ppos;
+    }
+    if ((dz & 1) == 0) return PairLoad<S, true>::ld(b + pos, inv[f], nz);
+    return PairLoad<S, false>::ld(b + pos, inv[f], nz);
+  }
+  __device__ __forceinline__ F2 m(int i) const {
+    if constexpr (G::NBX != 0) {
+      // beta1..3 = (beta + beta at x+1 / y+1 / z+1) * 0.5f, as media_fused_kernel
+      const float *b = (const float *)(xs[R] + G::NXF * G::HSLOT);
+      const F2 b0 = PairLoad<float, true>::ld(b + bpos, 1.f, nz);
+      F2 b1;
+      if (i == M_B1) b1 = PairLoad<float, true>::ld((const float *)(xs[R + 1] + G::NXF * G::HSLOT) + bpos, 1.f, nz);
+      else if (i == M_B2) b1 = PairLoad<float, true>::ld(b + bpos + G::BW, 1.f, nz);
+      else b1 = PairLoad<float, false>::ld(b + bpos + 1, 1.f, nz);
+      // the sum is rounded, then halved (a product of a sum: nothing to fuse)
+      return (b0 + b1) * f2(0.5f);
+    }
+    const float *b = (const float *)(cs + G::moff(G::midx(i)));
+    return PairLoad<float, true>::ld(b + ppos, 1.f, nz);
+  }
+};
+
+// Launch shape of a tiled sweep: 32 threads per consumer warp plus the
+// producer warp, and the resident CTAs per SM the register budget is sized
+// for.  Space order >= 6 keeps one CTA per SM (its rings fill shared memory),
+// so ptxas may use the whole register file rather than spill; the paired
+// evaluation at lower orders keeps two CTAs per SM.
+template <int R, typename S, int HET> struct TiledLaunch {
+  static constexpr int ZW = PairMode<S, HET>::v ? 1 : row_warps(R);
+  static constexpr int THREADS = 32 * (tile_rows(R) * ZW + 1);
+  static constexpr int MIN_BLOCKS = R >= 3 ? 1 : (PairMode<S, HET>::v ? 2 : 0);
+};
 
 // The literal table of a heterogeneous expression held as its few distinct
 // values (KMap): v[u] is the value of every literal with index map u.  The
@@ -264,6 +330,23 @@ template <int R, bool STRESS>
 struct KRegs {
   float v[KMap<R, STRESS>::NU];
   __device__ __forceinline__ float operator[](int i) const { return v[KMap<R, STRESS>::at(i)]; }
+};
+
+// The same for the paired evaluation: each distinct value as a pair {K, K},
+// with the -0 addend of the products (ofd_f32x2.cuh).
+template <int R, bool STRESS>
+struct KRegs2 {
+  F2 v[KMap<R, STRESS>::NU];
+  F2 nz;
+  __device__ __forceinline__ KF2 operator[](int i) const { return KF2{v[KMap<R, STRESS>::at(i)], nz}; }
+};
+
+// Literal table of the paired evaluation read from memory (tables that do not
+// follow KMap, e.g. grids with different spacings along the axes).
+struct KPairPtr {
+  const float *k;
+  F2 nz;
+  __device__ __forceinline__ KF2 operator[](int i) const { return KF2{f2(k[i]), nz}; }
 };
 
 // One CTA's work: tile `tile` (z fastest) of the 64 x 8 tiling, x chunk
@@ -343,13 +426,13 @@ __device__ __forceinline__ void sweep_tile(const SweepArgs<S> &a, const TiledPar
         const bool take_x = hissued < hlast && (pissued >= xe - 1 || hissued + 1 - R <= pissued + 1);
         if (take_x) {
           const int q = hissued + 1 - hq0;
-          if (!mbar_wait_or_abort(&xemp[q % G::NSH], (unsigned)((q / G::NSH - 1) & 1), &abort_flag)) break;
+          if (!mbar_wait_or_abort(&xemp[q % G::NSH], (unsigned)((q / G::NSH - 1) & 1), &abort_flag, p.wait_ns)) break;
           asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
           issue_x(hissued + 1);
           ++hissued;
         } else {
           const int q = pissued + 1 - xb;
-          if (!mbar_wait_or_abort(&cemp[q % G::NSC], (unsigned)((q / G::NSC - 1) & 1), &abort_flag)) break;
+          if (!mbar_wait_or_abort(&cemp[q % G::NSC], (unsigned)((q / G::NSC - 1) & 1), &abort_flag, p.wait_ns)) break;
           asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
           issue_c(pissued + 1);
           ++pissued;
@@ -368,12 +451,12 @@ __device__ __forceinline__ void sweep_tile(const SweepArgs<S> &a, const TiledPar
       bool ok = true;
       for (int pl = hwaited + 1; pl <= x + R && ok; ++pl) {
         const int q = pl - hq0;
-        if (!mbar_wait_or_abort(&xbar[q % G::NSH], (unsigned)((q / G::NSH) & 1), &abort_flag)) ok = false;
+        if (!mbar_wait_or_abort(&xbar[q % G::NSH], (unsigned)((q / G::NSH) & 1), &abort_flag, p.wait_ns)) ok = false;
         else hwaited = pl;
       }
       if (ok) {
         const int q = x - xb;
-        if (!mbar_wait_or_abort(&cbar[q % G::NSC], (unsigned)((q / G::NSC) & 1), &abort_flag)) ok = false;
+        if (!mbar_wait_or_abort(&cbar[q % G::NSC], (unsigned)((q / G::NSC) & 1), &abort_flag, p.wait_ns)) ok = false;
       }
       // leave as a whole warp (the release below is warp-synchronous)
       if (!__all_sync(0xffffffffu, ok)) {
@@ -383,33 +466,66 @@ __device__ __forceinline__ void sweep_tile(const SweepArgs<S> &a, const TiledPar
         }
         break;
       }
-      TiledAcc<R, S, HET, STRESS> A;
+      if constexpr (G::PAIR) {
+        // two adjacent z points per lane (z0 + 2 lane, + 1), f32x2 arithmetic
+        TiledAcc2<R, S, HET, STRESS> A;
 #pragma unroll
-      for (int k = 0; k < 2 * R + 1; ++k) A.xs[k] = xring + ((x + k - R - hq0) % G::NSH) * G::XSTAGE;
-      A.cs = cring + ((x - xb) % G::NSC) * G::CSTAGE;
-      A.inv = a.inv;
-#pragma unroll
-      for (int half = 0; half < 2 / G::ZW; ++half) {
-        const int zl = lane + 32 * (zpart + half);
+        for (int k = 0; k < 2 * R + 1; ++k) A.xs[k] = xring + ((x + k - R - hq0) % G::NSH) * G::XSTAGE;
+        A.cs = cring + ((x - xb) % G::NSC) * G::CSTAGE;
+        A.inv = a.inv;
+        A.nz = f2(a.nz);
+        const int zl = 2 * lane;
         const int z = z0 + zl;
         A.hpos = (yl + R) * G::HW + zl + G::ZH;
         A.ppos = yl * TZ + zl;
         A.bpos = yl * G::BW + zl;
         const long o = (long)x * g.plane + (long)y * g.P + z;
-        const bool inside = (z < g.n3 - g.m) && (y < g.n2 - g.m);
+        const bool in0 = (z < g.n3 - g.m) && (y < g.n2 - g.m);
+        const bool in1 = in0 && (z + 1 < g.n3 - g.m);
         if (STRESS) {
-          C out[6];
-          GenSweep<R, HET>::template stress<C>(A, K, out);
-          if (inside) {
+          F2 out[6];
+          GenSweep<R, HET>::template stress<F2>(A, K, out);
+          if (in0) {
 #pragma unroll
-            for (int i = 0; i < 6; ++i) a.out[F_TXX + i][o] = Storage<S>::store(out[i], a.sc[F_TXX + i]);
+            for (int i = 0; i < 6; ++i) PairStore<S>::st(a.out[F_TXX + i] + o, out[i], a.sc[F_TXX + i], in1);
           }
         } else {
-          C out[3];
-          GenSweep<R, HET>::template velocity<C>(A, K, out);
-          if (inside) {
+          F2 out[3];
+          GenSweep<R, HET>::template velocity<F2>(A, K, out);
+          if (in0) {
 #pragma unroll
-            for (int i = 0; i < 3; ++i) a.out[F_U + i][o] = Storage<S>::store(out[i], a.sc[F_U + i]);
+            for (int i = 0; i < 3; ++i) PairStore<S>::st(a.out[F_U + i] + o, out[i], a.sc[F_U + i], in1);
+          }
+        }
+      } else {
+        TiledAcc<R, S, HET, STRESS> A;
+#pragma unroll
+        for (int k = 0; k < 2 * R + 1; ++k) A.xs[k] = xring + ((x + k - R - hq0) % G::NSH) * G::XSTAGE;
+        A.cs = cring + ((x - xb) % G::NSC) * G::CSTAGE;
+        A.inv = a.inv;
+#pragma unroll
+        for (int half = 0; half < 2 / G::ZW; ++half) {
+          const int zl = lane + 32 * (zpart + half);
+          const int z = z0 + zl;
+          A.hpos = (yl + R) * G::HW + zl + G::ZH;
+          A.ppos = yl * TZ + zl;
+          A.bpos = yl * G::BW + zl;
+          const long o = (long)x * g.plane + (long)y * g.P + z;
+          const bool inside = (z < g.n3 - g.m) && (y < g.n2 - g.m);
+          if (STRESS) {
+            C out[6];
+            GenSweep<R, HET>::template stress<C>(A, K, out);
+            if (inside) {
+#pragma unroll
+              for (int i = 0; i < 6; ++i) a.out[F_TXX + i][o] = Storage<S>::store(out[i], a.sc[F_TXX + i]);
+            }
+          } else {
+            C out[3];
+            GenSweep<R, HET>::template velocity<C>(A, K, out);
+            if (inside) {
+#pragma unroll
+              for (int i = 0; i < 3; ++i) a.out[F_U + i][o] = Storage<S>::store(out[i], a.sc[F_U + i]);
+            }
           }
         }
       }
@@ -436,11 +552,26 @@ __device__ __forceinline__ void sweep_tile(const SweepArgs<S> &a, const TiledPar
   }
 }
 
-template <int R, typename S, int HET, bool STRESS>
-__global__ void __launch_bounds__(TiledThreads<R>::v, TiledMinBlocks<R>::v)
+// Single-handle sweep.  KD (paired evaluation only): the handle's literal
+// table follows KMap, and each thread holds its distinct values as register
+// pairs; otherwise pairs are formed from the table at every use.
+template <int R, typename S, int HET, bool STRESS, bool KD = false>
+__global__ void __launch_bounds__(TiledLaunch<R, S, HET>::THREADS, TiledLaunch<R, S, HET>::MIN_BLOCKS)
 sweep_tiled(const __grid_constant__ SweepArgs<S> a, const __grid_constant__ TiledParams p) {
   extern __shared__ unsigned char smem_raw[];
-  sweep_tile<R, S, HET, STRESS>(a, p, blockIdx.x, blockIdx.y, (const float *)a.K, smem_raw);
+  if constexpr (PairMode<S, HET>::v) {
+    if constexpr (KD) {
+      KRegs2<R, STRESS> kr;
+#pragma unroll
+      for (int i = 0; i < KMap<R, STRESS>::NK; ++i) kr.v[KMap<R, STRESS>::at(i)] = f2(a.K[i]);
+      kr.nz = f2(a.nz);
+      sweep_tile<R, S, HET, STRESS>(a, p, blockIdx.x, blockIdx.y, kr, smem_raw);
+    } else {
+      sweep_tile<R, S, HET, STRESS>(a, p, blockIdx.x, blockIdx.y, KPairPtr{a.K, f2(a.nz)}, smem_raw);
+    }
+  } else {
+    sweep_tile<R, S, HET, STRESS>(a, p, blockIdx.x, blockIdx.y, (const float *)a.K, smem_raw);
+  }
 }
 
 // One member of a grouped sweep launch: its arguments, descriptors and the
@@ -461,7 +592,7 @@ struct GroupSweep {
 // holds the distinct values in registers instead of reading the table from
 // global memory at every use.
 template <int R, typename S, int HET, bool STRESS, bool KD>
-__global__ void __launch_bounds__(TiledThreads<R>::v, TiledMinBlocks<R>::v)
+__global__ void __launch_bounds__(TiledLaunch<R, S, HET>::THREADS, TiledLaunch<R, S, HET>::MIN_BLOCKS)
 sweep_tiled_group(const GroupSweep<S> *__restrict__ tab, int n) {
   extern __shared__ unsigned char smem_raw[];
   __shared__ int s_member;
@@ -497,11 +628,20 @@ sweep_tiled_group(const GroupSweep<S> *__restrict__ tab, int n) {
     if (G::NBX) asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(&e.p.bmap) : "memory");
   }
   const int local = (int)blockIdx.x - e.cta_begin;
-  if constexpr (KD) {
+  if constexpr (KD && PairMode<S, HET>::v) {
+    KRegs2<R, STRESS> kr;
+#pragma unroll
+    for (int i = 0; i < KMap<R, STRESS>::NK; ++i) kr.v[KMap<R, STRESS>::at(i)] = f2(e.a.K[i]);
+    kr.nz = f2(e.a.nz);
+    sweep_tile<R, S, HET, STRESS>(e.a, e.p, local % e.tiles, local / e.tiles, kr, smem_raw);
+  } else if constexpr (KD) {
     KRegs<R, STRESS> kr;
 #pragma unroll
     for (int i = 0; i < KMap<R, STRESS>::NK; ++i) kr.v[KMap<R, STRESS>::at(i)] = e.a.K[i];
     sweep_tile<R, S, HET, STRESS>(e.a, e.p, local % e.tiles, local / e.tiles, kr, smem_raw);
+  } else if constexpr (PairMode<S, HET>::v) {
+    sweep_tile<R, S, HET, STRESS>(e.a, e.p, local % e.tiles, local / e.tiles, KPairPtr{e.a.K, f2(e.a.nz)},
+                                  smem_raw);
   } else {
     sweep_tile<R, S, HET, STRESS>(e.a, e.p, local % e.tiles, local / e.tiles, (const float *)e.a.K, smem_raw);
   }
@@ -544,6 +684,7 @@ void tiled_params(const SweepArgs<S> &a, const TiledCtx &ctx, int t0, int chunk_
     if (G::NBX) p.bmap = mp->beta;
   }
   p.err = ctx.err;
+  p.wait_ns = ctx.wait_ns;
   p.zcoord0 = ctx.z0 + g.m;
   const int nx = g.n1 - 2 * g.m, ny = g.n2 - 2 * g.m, nz = g.n3 - 2 * g.m;
   p.ntz = (nz + TZ - 1) / TZ;
@@ -569,8 +710,9 @@ void launch_tiled(const SweepArgs<S> &a, const TiledCtx &ctx, int t0, cudaStream
   TiledParams p;
   int tiles, chunks;
   tiled_params<R, S, HET, STRESS>(a, ctx, t0, 0, p, &tiles, &chunks);
-  auto kern = sweep_tiled<R, S, HET, STRESS>;
-  kern<<<dim3((unsigned)tiles, (unsigned)chunks), G::THREADS, G::SMEM, st>>>(a, p);
+  const dim3 grid((unsigned)tiles, (unsigned)chunks);
+  if (HET && ctx.kd[STRESS ? 1 : 0]) sweep_tiled<R, S, HET, STRESS, HET != 0><<<grid, G::THREADS, G::SMEM, st>>>(a, p);
+  else sweep_tiled<R, S, HET, STRESS, false><<<grid, G::THREADS, G::SMEM, st>>>(a, p);
 }
 
 // Dynamic shared memory opt-in of both sweeps; called once per handle so that
@@ -579,15 +721,21 @@ template <int R, typename S, int HET>
 void prepare_tiled() {
   if (tiled_fits<R, S, HET, true>()) {
     const int sm = TiledCfg<R, S, HET, true>::SMEM;
-    cudaFuncSetAttribute(sweep_tiled<R, S, HET, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    cudaFuncSetAttribute(sweep_tiled<R, S, HET, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
     cudaFuncSetAttribute(sweep_tiled_group<R, S, HET, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-    if constexpr (HET) cudaFuncSetAttribute(sweep_tiled_group<R, S, HET, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    if constexpr (HET) {
+      cudaFuncSetAttribute(sweep_tiled<R, S, HET, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+      cudaFuncSetAttribute(sweep_tiled_group<R, S, HET, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    }
   }
   if (tiled_fits<R, S, HET, false>()) {
     const int sm = TiledCfg<R, S, HET, false>::SMEM;
-    cudaFuncSetAttribute(sweep_tiled<R, S, HET, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    cudaFuncSetAttribute(sweep_tiled<R, S, HET, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
     cudaFuncSetAttribute(sweep_tiled_group<R, S, HET, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-    if constexpr (HET) cudaFuncSetAttribute(sweep_tiled_group<R, S, HET, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    if constexpr (HET) {
+      cudaFuncSetAttribute(sweep_tiled<R, S, HET, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+      cudaFuncSetAttribute(sweep_tiled_group<R, S, HET, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    }
   }
 }
 

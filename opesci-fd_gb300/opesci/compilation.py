@@ -28,12 +28,17 @@ class Compiler(object):
         self._cppargs = list(cppargs)
         self._ldargs = list(ldargs)
 
+    # language flag placed before the source (nvcc: '-x cu', so that a
+    # program written to a .cpp file, as the reference's model scripts name
+    # it, still compiles as CUDA)
+    _src_lang = ()
+
     def compile(self, src, out=None, shared=True):
         basename = os.path.splitext(src)[0]
         outname = out or ('%s.so' % basename if shared else basename)
         cpp = list(self._cppargs) + (['-Xcompiler', '-fPIC'] if shared else [])
         ld = (['-shared'] if shared else []) + list(self._ldargs)
-        cmd = [self._cc] + cpp + ['-o', outname, src] + ld
+        cmd = [self._cc] + cpp + ['-o', outname] + list(self._src_lang) + [src] + ld
         with open('%s.log' % basename, 'w') as log:
             log.write('Compiling: %s\n' % ' '.join(cmd))
             log.flush()
@@ -49,6 +54,8 @@ class Compiler(object):
 
 class NVCCCompiler(Compiler):
     """nvcc for sm_103a, linked against lib/libofd.so with an rpath."""
+
+    _src_lang = ('-x', 'cu')
 
     def __init__(self, cppargs=(), ldargs=()):
         lib = _build.build()   # the device runtime must exist before linking

@@ -84,8 +84,11 @@ def load_library():
         'ofd_set_media_const': [h, ctypes.c_float, ctypes.c_float, ctypes.c_float],
         'ofd_set_coefficients': [h, ctypes.c_int, fptr, ctypes.c_int, fptr, ctypes.c_int],
         'ofd_set_media': [h, fptr, fptr, fptr],
+        'ofd_set_media_async': [h, fptr, fptr, fptr],
         'ofd_upload_field': [h, ctypes.c_int, ctypes.c_int, fptr],
         'ofd_download_field': [h, ctypes.c_int, ctypes.c_int, fptr],
+        'ofd_upload_field_async': [h, ctypes.c_int, ctypes.c_int, fptr],
+        'ofd_download_field_async': [h, ctypes.c_int, ctypes.c_int, fptr],
         'ofd_upload_field_device': [h, ctypes.c_int, ctypes.c_int, ctypes.c_void_p],
         'ofd_download_field_device': [h, ctypes.c_int, ctypes.c_int, ctypes.c_void_p],
         'ofd_zero_fields': [h],
@@ -96,6 +99,7 @@ def load_library():
         'ofd_step': [h, ctypes.c_int],
         'ofd_step_graph': [h, ctypes.c_int],
         'ofd_set_persistent': [h, ctypes.c_int],
+        'ofd_set_wait_limit': [h, ctypes.c_double],
         'ofd_step_timed': [h, ctypes.c_int, P(ctypes.c_double), P(ctypes.c_long)],
         'ofd_set_tuning': [h, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int],
         'ofd_step_profiled': [h, ctypes.c_int, P(ctypes.c_double), P(ctypes.c_double), P(ctypes.c_long)],
@@ -278,6 +282,26 @@ class Simulation(object):
         _check(self.lib.ofd_download_field(self.h, f, level, _fptr(out)), 'ofd_download_field')
         return out
 
+    def download_all_async(self, outs, level=None):
+        """Queue the download of all nine fields of a level into ``outs``
+        (nine float32 arrays of the grid's dims, ideally pinned); they are
+        filled once sync() returns."""
+        if level is None:
+            level = self.steps % 2
+        for i, o in enumerate(outs):
+            if o.dtype != np.float32 or o.shape != self.dims or not o.flags['C_CONTIGUOUS']:
+                raise ValueError('download buffers must be C-contiguous float32 arrays of shape %s' % (self.dims,))
+            _check(self.lib.ofd_download_field_async(self.h, i, level, _fptr(o)), 'ofd_download_field_async')
+
+    def set_media_async(self, rho, vp, vs):
+        """ofd_set_media queued without waiting; the arrays must stay alive
+        (and unchanged) until sync()."""
+        arrs = [np.asarray(a) for a in (rho, vp, vs)]
+        for a in arrs:
+            if a.dtype != np.float32 or a.shape != self.dims or not a.flags['C_CONTIGUOUS']:
+                raise ValueError('media arrays must be C-contiguous float32 arrays of shape %s' % (self.dims,))
+        _check(self.lib.ofd_set_media_async(self.h, *[_fptr(a) for a in arrs]), 'ofd_set_media_async')
+
     def zero(self):
         _check(self.lib.ofd_zero_fields(self.h), 'ofd_zero_fields')
 
@@ -321,6 +345,12 @@ class Simulation(object):
     def set_persistent(self, enable=True):
         """Run time steps in cooperative launches of up to 1024 steps."""
         _check(self.lib.ofd_set_persistent(self.h, 1 if enable else 0), 'ofd_set_persistent')
+
+    def set_wait_limit(self, seconds):
+        """Limit of every device-side wait of this simulation's kernels (TMA
+        pipeline waits, grid barriers); expiry makes the next sync raise
+        OFDError with code OFD_ETIMEOUT."""
+        _check(self.lib.ofd_set_wait_limit(self.h, float(seconds)), 'ofd_set_wait_limit')
 
     def set_tuning(self, stress_variant=0, velocity_variant=0, chunk_waves=1, plain_bx=32, plain_by=8,
                    persistent=0):

@@ -18,6 +18,16 @@ work overlaps on the device, and a finished request frees its memory for the
 queue.  The baseline serves the same stream one request at a time with
 per-kernel launches.
 
+Failures are contained per request.  A request may be cancelled
+(Request.cancel(), from any thread) or carry a deadline (seconds after its
+arrival); a queued one is dropped, an admitted one is stopped at its next
+slice boundary (after its last launched work has completed) and its memory
+returns to the budget.  A request whose device state cannot be created at
+admission (an allocation failure or any other error of the runtime) is
+answered as failed with the error text, and serving goes on.  Each request
+ends with status 'done', 'cancelled', 'expired' or 'failed'; latency and
+throughput figures count the 'done' ones.
+
     python -m opesci.serve --requests 40 --rates 0.5 1 2
 
 prints a JSON object: per rate, p50/p99 latency and aggregate GLUP/s for both
@@ -43,13 +53,30 @@ FP16_SCALES = [2.0 ** 30] * 3 + [2.0 ** 9] * 3 + [2.0 ** 10] * 3
 
 
 class Request(object):
-    def __init__(self, rid, arrival, shot, storage):
+    def __init__(self, rid, arrival, shot, storage, deadline=None):
         self.id, self.arrival, self.shot, self.storage = rid, arrival, shot, storage
+        self.deadline = deadline          # seconds after arrival, or None
         self.admitted = self.finished = None
+        self.status = None                # 'done', 'cancelled', 'expired', 'failed'
+        self.error = None
+        self.cancelled = False
 
     @property
     def lups(self):
         return self.shot.lups
+
+    def cancel(self):
+        """Ask the server to drop this request (safe from another thread)."""
+        self.cancelled = True
+
+    def stop_reason(self, now):
+        """'cancelled' / 'expired' when the request should stop at ``now``
+        (server clock), else None."""
+        if self.cancelled:
+            return 'cancelled'
+        if self.deadline is not None and now > self.arrival + self.deadline:
+            return 'expired'
+        return None
 
 
 def make_requests(count, rate, seed=0, edge_range=(48, 384), so_choices=(4, 8), steps_range=(200, 2000),
@@ -93,17 +120,59 @@ def open_request(req, built, tuned=True):
     return sim
 
 
-def _finish_stats(reqs, t_first, t_last):
-    lat = np.array([r.finished - r.arrival for r in reqs])
-    lups = sum(r.lups for r in reqs)
-    return {'p50_s': float(np.percentile(lat, 50)), 'p99_s': float(np.percentile(lat, 99)),
-            'mean_s': float(lat.mean()), 'glups': lups / (t_last - t_first) / 1e9,
-            'makespan_s': t_last - t_first}
+def _finish_stats(reqs, t_first=None, t_last=None):
+    done = [r for r in reqs if r.status == 'done']
+    counts = {k: sum(1 for r in reqs if r.status == k) for k in ('done', 'cancelled', 'expired', 'failed')}
+    if not done:
+        return dict(counts, p50_s=None, p99_s=None, mean_s=None, glups=0.0, makespan_s=None)
+    t_first = min(r.arrival for r in reqs) if t_first is None else t_first
+    t_last = max(r.finished for r in reqs if r.finished is not None) if t_last is None else t_last
+    lat = np.array([r.finished - r.arrival for r in done])
+    lups = sum(r.lups for r in done)
+    return dict(counts, p50_s=float(np.percentile(lat, 50)), p99_s=float(np.percentile(lat, 99)),
+                mean_s=float(lat.mean()), glups=lups / max(t_last - t_first, 1e-12) / 1e9,
+                makespan_s=t_last - t_first)
 
 
-def serve_continuous(reqs, built, budget_bytes=150e9, slice_steps=32, max_active=96, checks=None):
+def _end(req, status, now, error=None):
+    req.status, req.finished = status, now
+    if error is not None:
+        req.error = error
+
+
+def _admit(queue, active, used, budget_bytes, max_active, now, opener, built, footprint_fn, extra):
+    """Move queued requests into ``active`` while the budget allows; drops
+    cancelled/expired ones and answers requests whose device state cannot be
+    created as failed.  Returns the new byte count in use."""
+    while queue and len(active) < max_active:
+        r = queue[0]
+        why = r.stop_reason(now)
+        if why:
+            queue.popleft()
+            _end(r, why, now)
+            continue
+        fp = footprint_fn(r)
+        if active and used + fp > budget_bytes:
+            break
+        queue.popleft()
+        r.admitted = now
+        try:
+            sim = opener(r, built[r.id])
+        except Exception as e:   # the request fails, the server goes on
+            _end(r, 'failed', now, '%s: %s' % (type(e).__name__, e))
+            continue
+        active.append([r, sim, r.shot.steps, fp] + list(extra))
+        used += fp
+    return used
+
+
+def serve_continuous(reqs, built, budget_bytes=150e9, slice_steps=32, max_active=96, checks=None,
+                     opener=None, footprint_fn=footprint):
     """Continuous batching.  ``checks`` (dict) receives each request's FP64
-    sums of squares of its final fields."""
+    sums of squares of its final fields.  ``opener(req, built)`` creates a
+    request's device state (default: open_request with autotuned launch
+    knobs)."""
+    opener = opener or open_request
     t0 = time.perf_counter()
     pending = deque(sorted(reqs, key=lambda r: r.arrival))
     queue = deque()
@@ -113,28 +182,30 @@ def serve_continuous(reqs, built, budget_bytes=150e9, slice_steps=32, max_active
         now = time.perf_counter() - t0
         while pending and pending[0].arrival <= now:
             queue.append(pending.popleft())
-        while queue and len(active) < max_active:
-            r = queue[0]
-            fp = footprint(r)
-            if active and used + fp > budget_bytes:
-                break
-            queue.popleft()
-            r.admitted = time.perf_counter() - t0
-            active.append([r, open_request(r, built[r.id]), r.shot.steps, fp])
-            used += fp
+        used = _admit(queue, active, used, budget_bytes, max_active, now, opener, built, footprint_fn, ())
         if not active:
             if pending:
                 time.sleep(max(0.0, pending[0].arrival - (time.perf_counter() - t0)))
+            elif queue:
+                time.sleep(50e-6)
             continue
         progressed = False
         for a in list(active):
             r, sim, rem, fp = a
             if sim.done():
-                if rem == 0:
-                    sim.sync()          # raises if any device wait of the request expired
-                    r.finished = time.perf_counter() - t0
-                    if checks is not None:
-                        checks[r.id] = sim.sumsq().tolist()
+                now = time.perf_counter() - t0
+                why = r.stop_reason(now) if rem > 0 else None
+                if rem == 0 or why:
+                    try:
+                        sim.sync()          # raises if a device wait of the request expired
+                        if why:
+                            _end(r, why, now)
+                        else:
+                            _end(r, 'done', time.perf_counter() - t0)
+                            if checks is not None:
+                                checks[r.id] = sim.sumsq().tolist()
+                    except Exception as e:
+                        _end(r, 'failed', time.perf_counter() - t0, '%s: %s' % (type(e).__name__, e))
                     sim.close()
                     used -= fp
                     active.remove(a)
@@ -146,12 +217,11 @@ def serve_continuous(reqs, built, budget_bytes=150e9, slice_steps=32, max_active
                 progressed = True
         if not progressed:
             time.sleep(50e-6)
-    t_first = min(r.arrival for r in reqs)
-    t_last = max(r.finished for r in reqs)
-    return _finish_stats(reqs, t_first, t_last)
+    return _finish_stats(reqs)
 
 
-def serve_grouped(reqs, built, budget_bytes=150e9, slice_steps=32, max_active=256, checks=None):
+def serve_grouped(reqs, built, budget_bytes=150e9, slice_steps=32, max_active=256, checks=None,
+                  opener=None, footprint_fn=footprint, grouper=None):
     """Continuous batching on groups.  Admission as in serve_continuous; the
     admitted requests advance in rounds: each round groups the requests
     that still have steps to run by space order, storage and time-level
@@ -159,7 +229,12 @@ def serve_grouped(reqs, built, budget_bytes=150e9, slice_steps=32, max_active=25
     group) and advances every group by min(slice_steps, its smallest
     remaining count) steps.  Up to two rounds are in flight; a request
     that arrives joins the next round, one that finishes is answered and
-    freed when its last round has completed."""
+    freed when its last round has completed.  A cancelled or expired
+    request joins no further round and is freed when its last round has
+    completed.  ``opener`` and ``grouper`` (sims -> groups) default to the
+    device runtime's."""
+    opener = opener or (lambda r, b: open_request(r, b, tuned=False))
+    grouper = grouper or runtime.make_groups
     t0 = time.perf_counter()
     pending = deque(sorted(reqs, key=lambda r: r.arrival))
     queue = deque()
@@ -172,34 +247,45 @@ def serve_grouped(reqs, built, budget_bytes=150e9, slice_steps=32, max_active=25
         now = time.perf_counter() - t0
         while pending and pending[0].arrival <= now:
             queue.append(pending.popleft())
-        while queue and len(active) < max_active:
-            r = queue[0]
-            fp = footprint(r)
-            if active and used + fp > budget_bytes:
-                break
-            queue.popleft()
-            r.admitted = time.perf_counter() - t0
-            active.append([r, open_request(r, built[r.id], tuned=False), r.shot.steps, fp, -1])
-            used += fp
+        used = _admit(queue, active, used, budget_bytes, max_active, now, opener, built, footprint_fn, (-1,))
         # retire rounds that have finished (oldest first)
         while rounds and all(g.done() for g in rounds[0][1]):
             rid, groups = rounds.popleft()
+            failed = None
             for g in groups:
-                g.sync()
+                try:
+                    g.sync()
+                except Exception as e:   # a member's device wait expired
+                    failed = '%s: %s' % (type(e).__name__, e)
                 g.close()
+            if failed:
+                for a in active:
+                    if a[4] == rid:
+                        a[0].error = failed
             completed = rid
-        # answer requests whose last round has completed
+        # answer requests whose last round has completed; stop cancelled or
+        # expired ones there
+        now = time.perf_counter() - t0
         for a in list(active):
             r, sim, rem, fp, last = a
-            if rem == 0 and last <= completed:
-                sim.sync()
-                r.finished = time.perf_counter() - t0
-                if checks is not None:
-                    checks[r.id] = sim.sumsq().tolist()
+            why = r.stop_reason(now) if rem > 0 else None
+            if (rem == 0 or why) and last <= completed:
+                try:
+                    sim.sync()
+                    if r.error:
+                        raise RuntimeError(r.error)
+                    if why:
+                        _end(r, why, now)
+                    else:
+                        _end(r, 'done', time.perf_counter() - t0)
+                        if checks is not None:
+                            checks[r.id] = sim.sumsq().tolist()
+                except Exception as e:
+                    _end(r, 'failed', time.perf_counter() - t0, '%s: %s' % (type(e).__name__, e))
                 sim.close()
                 used -= fp
                 active.remove(a)
-        live = [a for a in active if a[2] > 0]
+        live = [a for a in active if a[2] > 0 and not a[0].stop_reason(now)]
         if live and len(rounds) < 2:
             classes = {}
             for a in live:
@@ -208,7 +294,7 @@ def serve_grouped(reqs, built, budget_bytes=150e9, slice_steps=32, max_active=25
             groups = []
             for members in classes.values():
                 k = min(slice_steps, min(a[2] for a in members))
-                for g in runtime.make_groups([a[1] for a in members]):
+                for g in grouper([a[1] for a in members]):
                     g.step(k)
                     groups.append(g)
                 for a in members:
@@ -217,13 +303,11 @@ def serve_grouped(reqs, built, budget_bytes=150e9, slice_steps=32, max_active=25
             rounds.append((next_round, groups))
             next_round += 1
             continue
-        if not active and pending:
+        if not active and not queue and pending:
             time.sleep(max(0.0, pending[0].arrival - (time.perf_counter() - t0)))
         else:
             time.sleep(50e-6)
-    t_first = min(r.arrival for r in reqs)
-    t_last = max(r.finished for r in reqs)
-    return _finish_stats(reqs, t_first, t_last)
+    return _finish_stats(reqs)
 
 
 def serve_one_by_one(reqs, built, checks=None):
@@ -237,13 +321,11 @@ def serve_one_by_one(reqs, built, checks=None):
         sim = open_request(r, built[r.id], tuned=False)
         sim.step(r.shot.steps)
         sim.sync()
-        r.finished = time.perf_counter() - t0
+        _end(r, 'done', time.perf_counter() - t0)
         if checks is not None:
             checks[r.id] = sim.sumsq().tolist()
         sim.close()
-    t_first = min(r.arrival for r in reqs)
-    t_last = max(r.finished for r in reqs)
-    return _finish_stats(reqs, t_first, t_last)
+    return _finish_stats(reqs)
 
 
 def max_rel_diff(a, b):

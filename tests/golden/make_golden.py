@@ -1,8 +1,10 @@
 """Regenerate the golden fixtures of this directory from the reference.
 
-Run in a container that has the reference checkout (default /root/reference):
+Run where the reference checkout is present (argument --reference, the
+OPESCI_REFERENCE environment variable, or the directory "reference" beside
+this repository):
 
-    python tests/golden/make_golden.py [--reference /root/reference]
+    python tests/golden/make_golden.py [--reference <dir>]
 
 Writes
   test3d_l2.json          the nine L2 norms printed by the reference's own
@@ -123,7 +125,8 @@ def segy_fixtures():
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument('--reference', default='/root/reference')
+    ap.add_argument('--reference', default=os.environ.get('OPESCI_REFERENCE', os.path.join(os.path.dirname(ROOT), 'reference')),
+                    help='reference checkout (default: $OPESCI_REFERENCE, else "reference" beside this repository)')
     ap.add_argument('--threads', type=int, default=os.cpu_count())
     ap.add_argument('--only', choices=['resample', 'segy'], default=None)
     args = ap.parse_args()

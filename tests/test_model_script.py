@@ -1,0 +1,80 @@
+"""The reference's own model script, tests/eigenwave3d.py, run against this
+package with only two edits: its Python-2 print statements become print()
+calls, and the compiler it selects is 'nvcc' (given on its own command line,
+``-c nvcc``).  Nothing else of the script changes.
+
+The script is not copied into this repository: the test reads it from the
+reference checkout (the OPESCI_REFERENCE environment variable, else the
+directory "reference" beside this repository), applies the print edit in
+memory, writes the result to a temporary directory and runs it there (the
+script writes its generated program next to itself, under src/).  Without
+the checkout the test is skipped.
+
+On CPU the script's default mode runs the whole flow up to the executable:
+the 100^3 eigenwave model is declared through SField/VField/StaggeredGrid,
+solved, given free surfaces, its kernel AI is printed, and the generated
+CUDA program is built by nvcc for sm_103a.  Executing it (-x) needs a GPU.
+"""
+import os
+import re
+import subprocess
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+PKG = os.path.join(ROOT, 'opesci-fd_gb300')
+
+
+def reference_dir():
+    return os.environ.get('OPESCI_REFERENCE', os.path.join(os.path.dirname(ROOT), 'reference'))
+
+
+_PRINT = re.compile(r'^(\s*)print (.+?)\s*$')
+
+
+def py3_prints(text):
+    """Python-2 print statements -> print() calls (the only source edit)."""
+    out = []
+    for line in text.split('\n'):
+        m = _PRINT.match(line)
+        out.append('%sprint(%s)' % (m.group(1), m.group(2)) if m else line)
+    return '\n'.join(out)
+
+
+def edited_script(tmp_path):
+    src = os.path.join(reference_dir(), 'tests', 'eigenwave3d.py')
+    if not os.path.exists(src):
+        pytest.skip('reference checkout not present')
+    text = py3_prints(open(src).read())
+    compile(text, 'eigenwave3d.py', 'exec')   # valid Python 3 after the print edit alone
+    dst = tmp_path / 'eigenwave3d.py'
+    dst.write_text(text)
+    (tmp_path / 'src').mkdir()
+    return dst
+
+
+def test_print_edit_is_the_only_change(tmp_path):
+    src = os.path.join(reference_dir(), 'tests', 'eigenwave3d.py')
+    if not os.path.exists(src):
+        pytest.skip('reference checkout not present')
+    before = open(src).read().split('\n')
+    after = py3_prints('\n'.join(before)).split('\n')
+    changed = [(a, b) for a, b in zip(before, after) if a != b]
+    assert len(before) == len(after)
+    assert changed and all(b.strip().startswith('print(') and a.strip().startswith('print ') for a, b in changed)
+
+
+@pytest.mark.skipif(not (os.path.exists('/usr/local/cuda/bin/nvcc') or
+                         subprocess.run(['which', 'nvcc'], capture_output=True).returncode == 0),
+                    reason='needs nvcc')
+def test_default_mode_builds_with_nvcc(tmp_path):
+    script = edited_script(tmp_path)
+    env = dict(os.environ, PYTHONPATH=PKG + os.pathsep + os.environ.get('PYTHONPATH', ''))
+    r = subprocess.run([sys.executable, str(script), 'default', '-c', 'nvcc'], cwd=str(tmp_path), env=env,
+                       capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-3000:]
+    assert 'require dt < ' in r.stdout
+    assert 'Compiled:' in r.stdout
+    exe = tmp_path / 'src' / 'eigenwave3d'
+    assert exe.exists(), r.stdout[-2000:]
