@@ -57,7 +57,17 @@ typedef struct ofd_config {
     double weights[4];     /* staggered first-derivative weights c_1..c_R (R = space_order/2) */
     float field_scale[9];  /* stored = value * scale (16-bit storage; powers of two; 0 = 1) */
     int kernel_variant;    /* 0 = best available, 1 = plain (one thread per column) */
+    int rounding;          /* 16-bit storage: enum ofd_rounding of the sweeps' stores */
 } ofd_config;
+
+/* Rounding of the values the sweeps store in 16-bit fields (no counterpart in
+ * the reference, which stores float or double).  Stochastic rounding stores
+ * the upper neighbour of v with probability (v - lower) / (upper - lower),
+ * from a deterministic hash of (element, field, step): the same bits on every
+ * kernel path and run, and v in expectation, so increments below half a unit
+ * in the last place are not lost.  Ghost cells and the source use
+ * round-to-nearest.  FP32 and FP64 storage ignore the mode. */
+enum ofd_rounding { OFD_ROUND_NEAREST = 0, OFD_ROUND_STOCHASTIC = 1 };
 
 typedef struct ofd_handle ofd_handle;
 

@@ -36,16 +36,8 @@ __device__ __forceinline__ F2 f2(float lo, float hi) {
 }
 __device__ __forceinline__ F2 f2(float a) { return f2(a, a); }
 
-__device__ __forceinline__ float f2_lo(F2 a) {
-  float lo, hi;
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a.v));
-  return lo;
-}
-__device__ __forceinline__ float f2_hi(F2 a) {
-  float lo, hi;
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a.v));
-  return hi;
-}
+__device__ __forceinline__ float f2_lo(F2 a) { return __uint_as_float((unsigned)(a.v & 0xffffffffULL)); }
+__device__ __forceinline__ float f2_hi(F2 a) { return __uint_as_float((unsigned)(a.v >> 32)); }
 
 __device__ __forceinline__ F2 operator*(F2 a, F2 b) {
   F2 r;
@@ -142,15 +134,22 @@ template <bool ALIGNED> struct PairLoad<__nv_bfloat16, ALIGNED> {
 // The stored value is value * sc rounded to S, as Storage<S>::store.
 template <typename S> struct PairStore;
 
+// sr: stochastic rounding of 16-bit stores (SweepStore) with the hash of
+// element offsets o, o + 1 of field f at step.
 template <> struct PairStore<float> {
-  __device__ __forceinline__ static void st(float *p, F2 v, float, bool both) {
+  __device__ __forceinline__ static void st(float *p, F2 v, float, bool both, int, long, int, long) {
     if (both) *reinterpret_cast<float2 *>(p) = make_float2(f2_lo(v), f2_hi(v));
     else p[0] = f2_lo(v);
   }
 };
 
 template <> struct PairStore<__half> {
-  __device__ __forceinline__ static void st(__half *p, F2 v, float sc, bool both) {
+  __device__ __forceinline__ static void st(__half *p, F2 v, float sc, bool both, int sr, long o, int f, long step) {
+    if (sr) {
+      p[0] = SweepStore<__half>::st(f2_lo(v), sc, 1, sr_hash(o, f, step));
+      if (both) p[1] = SweepStore<__half>::st(f2_hi(v), sc, 1, sr_hash(o + 1, f, step));
+      return;
+    }
     const F2 s = v * f2(sc);
     if (both) *reinterpret_cast<__half2 *>(p) = __floats2half2_rn(f2_lo(s), f2_hi(s));
     else p[0] = __float2half_rn(f2_lo(s));
@@ -158,7 +157,13 @@ template <> struct PairStore<__half> {
 };
 
 template <> struct PairStore<__nv_bfloat16> {
-  __device__ __forceinline__ static void st(__nv_bfloat16 *p, F2 v, float sc, bool both) {
+  __device__ __forceinline__ static void st(__nv_bfloat16 *p, F2 v, float sc, bool both, int sr, long o, int f,
+                                            long step) {
+    if (sr) {
+      p[0] = SweepStore<__nv_bfloat16>::st(f2_lo(v), sc, 1, sr_hash(o, f, step));
+      if (both) p[1] = SweepStore<__nv_bfloat16>::st(f2_hi(v), sc, 1, sr_hash(o + 1, f, step));
+      return;
+    }
     const F2 s = v * f2(sc);
     if (both) *reinterpret_cast<__nv_bfloat162 *>(p) = __floats2bfloat162_rn(f2_lo(s), f2_hi(s));
     else p[0] = __float2bfloat16_rn(f2_lo(s));

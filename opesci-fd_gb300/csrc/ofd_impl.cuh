@@ -44,6 +44,7 @@ struct DevState {
   int persistent;      // 1: time steps run in one cooperative launch
   unsigned *d_bar;     // grid-barrier words of the persistent kernel
   int het;             // 1: media arrays are factors of the update (read mode)
+  int sr;              // 16-bit storage: stochastic rounding of the sweeps' stores
   int nks, nkv;        // literal-table sizes (0 until ofd_set_coefficients)
   float Ks[OFD_MAX_K], Kv[OFD_MAX_K];
 };
@@ -227,6 +228,8 @@ struct Impl : Backend {
     a.ih3 = (C)(1.0 / s.h[2]);
     for (int k = 0; k < 4; ++k) a.c[k] = (C)s.c[k];
     a.xchunk = 0;
+    a.sr = (s.sr && sizeof(S) == 2) ? 1 : 0;
+    a.step = s.d_step;
     a.nz = -0.0f;
     const float *K = stress ? s.Ks : s.Kv;
     const int nk = stress ? s.nks : s.nkv;

@@ -102,8 +102,12 @@ __global__ void __launch_bounds__(256) persistent_steps_kernel(const __grid_cons
   const long gstride = (long)gridDim.x * blockDim.x;
   const int nx = g.n1 - 2 * g.m, ny = g.n2 - 2 * g.m, nz = g.n3 - 2 * g.m;
   const long npts = (long)nx * ny * nz;
+  // the step count before this launch (read by every block before the first
+  // grid barrier; block 0 advances the counter only after it)
+  const long step0 = *(volatile long *)a.d_step;
   for (int k = 0; k < a.nsteps; ++k) {
     const int p = (a.p0 + k) & 1;
+    const long step = step0 + k;
     // stress sweep
     {
       const SweepArgs<S> &sa = a.st[p];
@@ -117,7 +121,9 @@ __global__ void __launch_bounds__(256) persistent_steps_kernel(const __grid_cons
         C out[6];
         GenSweep<R, HET>::template stress<C>(A, (const float *)sa.K, out);
 #pragma unroll
-        for (int f = 0; f < 6; ++f) sa.out[F_TXX + f][o] = Storage<S>::store(out[f], sa.sc[F_TXX + f]);
+        for (int f = 0; f < 6; ++f)
+          sa.out[F_TXX + f][o] =
+              SweepStore<S>::st(out[f], sa.sc[F_TXX + f], sa.sr, sa.sr ? sr_hash(o, F_TXX + f, step) : 0u);
       }
     }
     if (!grid_barrier(a.bar, a.err, a.wait_ns)) return;
@@ -149,7 +155,8 @@ __global__ void __launch_bounds__(256) persistent_steps_kernel(const __grid_cons
         C out[3];
         GenSweep<R, HET>::template velocity<C>(A, (const float *)va.K, out);
 #pragma unroll
-        for (int f = 0; f < 3; ++f) va.out[F_U + f][o] = Storage<S>::store(out[f], va.sc[F_U + f]);
+        for (int f = 0; f < 3; ++f)
+          va.out[F_U + f][o] = SweepStore<S>::st(out[f], va.sc[F_U + f], va.sr, va.sr ? sr_hash(o, F_U + f, step) : 0u);
       }
     }
     if (!grid_barrier(a.bar, a.err, a.wait_ns)) return;

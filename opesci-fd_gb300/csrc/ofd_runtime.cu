@@ -43,50 +43,50 @@ int fail_msg(int code, const char *msg) { return fail(code, "%s", msg); }
 // grid with upper neighbours clamped at the last index: beta = 1/rho,
 // lambda = rho (vp^2 - 2 vs^2), mu = rho vs^2; beta1..3 the means of beta and
 // its upper neighbour along x/y/z; mu12/13/23 the harmonic means of mu over
-// the four points of the cell edge (1/mu in double).  One pass: beta, lambda,
-// mu and 1/mu are recomputed at the upper neighbours from rho, vp, vs rather
-// than read back from intermediate arrays.  Thread (z, y) of block row (y, x)
-// handles one point; no index divisions.
-__device__ __forceinline__ void media_point(const float *rho, const float *vp, const float *vs, long i, float *beta,
-                                            float *lam, float *mu, double *inv_mu) {
-  const double r = rho[i], p = vp[i], s = vs[i];
-  *beta = (float)(1.0 / r);
-  *lam = (float)(r * (p * p - 2.0 * (s * s)));
+// the four points of the cell edge (1/mu in double).  Two passes over a 3D
+// grid of (z, y) blocks per x plane (no index divisions): the point values,
+// then the averages.  FP64 division is the cost on this GPU (its FP64 rate is
+// a small fraction of FP32), so each 1/mu is computed once per point and
+// beta as a float division: (float)(1.0/(double)rho) equals the correctly
+// rounded float quotient 1.0f/rho, since rounding a quotient of 24-bit
+// operands first to 53 bits and then to 24 bits is innocuous (53 >= 2*24+2;
+// S. A. Figueroa, "When is double rounding innocuous?", SIGNUM 1995).
+__global__ void media_point_kernel(const float *__restrict__ rho, const float *__restrict__ vp,
+                                   const float *__restrict__ vs, Geom g, float *o_beta, float *o_lam, float *o_mu,
+                                   double *inv_mu) {
+  const int z = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int x = blockIdx.z;
+  if (z >= g.n3 || y >= g.n2) return;
+  const long i = ((long)x * g.n2 + y) * g.n3 + z;
+  const long o = (long)x * g.plane + (long)y * g.P + z;
+  const float rf = rho[i];
+  const double r = rf, p = vp[i], s = vs[i];
+  o_beta[o] = __fdiv_rn(1.0f, rf);
+  o_lam[o] = (float)(r * (p * p - 2.0 * (s * s)));
   const float m = (float)(r * (s * s));
-  *mu = m;
-  *inv_mu = 1.0 / (double)m;
+  o_mu[o] = m;
+  inv_mu[i] = 1.0 / (double)m;
 }
 
-__global__ void media_fused_kernel(const float *__restrict__ rho, const float *__restrict__ vp,
-                                   const float *__restrict__ vs, Geom g, float *o_lam, float *o_mu, float *o_mu12,
-                                   float *o_mu13, float *o_mu23, float *o_b1, float *o_b2, float *o_b3,
-                                   float *o_beta) {
+__global__ void media_avg_kernel(const float *o_beta_in, const double *__restrict__ im, Geom g, float *o_mu12,
+                                 float *o_mu13, float *o_mu23, float *o_b1, float *o_b2, float *o_b3) {
   const int z = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int x = blockIdx.z;
   if (z >= g.n3 || y >= g.n2) return;
   const int x1 = x + 1 < g.n1 ? x + 1 : x, y1 = y + 1 < g.n2 ? y + 1 : y, z1 = z + 1 < g.n3 ? z + 1 : z;
   auto D = [&](int a, int b, int c) { return ((long)a * g.n2 + b) * g.n3 + c; };
-  float b0, l0, m0f, bx, by, bz, lt, mt;
-  double im0, imx, imy, imz, imxy, imxz, imyz;
-  media_point(rho, vp, vs, D(x, y, z), &b0, &l0, &m0f, &im0);
-  media_point(rho, vp, vs, D(x1, y, z), &bx, &lt, &mt, &imx);
-  media_point(rho, vp, vs, D(x, y1, z), &by, &lt, &mt, &imy);
-  media_point(rho, vp, vs, D(x, y, z1), &bz, &lt, &mt, &imz);
-  float bt;
-  media_point(rho, vp, vs, D(x1, y1, z), &bt, &lt, &mt, &imxy);
-  media_point(rho, vp, vs, D(x1, y, z1), &bt, &lt, &mt, &imxz);
-  media_point(rho, vp, vs, D(x, y1, z1), &bt, &lt, &mt, &imyz);
-  const long o = (long)x * g.plane + (long)y * g.P + z;
-  o_lam[o] = l0;
-  o_mu[o] = m0f;
-  o_beta[o] = b0;
-  o_b1[o] = (b0 + bx) * 0.5f;
-  o_b2[o] = (b0 + by) * 0.5f;
-  o_b3[o] = (b0 + bz) * 0.5f;
-  o_mu12[o] = (float)(1.0 / (0.25 * (im0 + imx + imy + imxy)));
-  o_mu13[o] = (float)(1.0 / (0.25 * (im0 + imx + imz + imxz)));
-  o_mu23[o] = (float)(1.0 / (0.25 * (im0 + imy + imz + imyz)));
+  auto O = [&](int a, int b, int c) { return (long)a * g.plane + (long)b * g.P + c; };
+  const long o = O(x, y, z);
+  const float b0 = o_beta_in[o];
+  o_b1[o] = (b0 + o_beta_in[O(x1, y, z)]) * 0.5f;
+  o_b2[o] = (b0 + o_beta_in[O(x, y1, z)]) * 0.5f;
+  o_b3[o] = (b0 + o_beta_in[O(x, y, z1)]) * 0.5f;
+  const double m0 = im[D(x, y, z)], mx = im[D(x1, y, z)], my = im[D(x, y1, z)], mz = im[D(x, y, z1)];
+  o_mu12[o] = (float)(1.0 / (0.25 * (m0 + mx + my + im[D(x1, y1, z)])));
+  o_mu13[o] = (float)(1.0 / (0.25 * (m0 + mx + mz + im[D(x1, y, z1)])));
+  o_mu23[o] = (float)(1.0 / (0.25 * (m0 + my + mz + im[D(x, y1, z1)])));
 }
 
 __global__ void fill_kernel(float *p, long n, float v) {
@@ -156,6 +156,8 @@ int check_config(const ofd_config *c) {
   if (!(c->dt > 0)) return fail(OFD_EINVAL, "dt must be > 0");
   for (int i = 0; i < 6; ++i)
     if (c->free_surface[i] < 0 || c->free_surface[i] > 2) return fail(OFD_EINVAL, "bad free_surface[%d]", i);
+  if (c->rounding != OFD_ROUND_NEAREST && c->rounding != OFD_ROUND_STOCHASTIC)
+    return fail(OFD_EINVAL, "unknown rounding mode %d", c->rounding);
   return OFD_OK;
 }
 
@@ -360,6 +362,7 @@ int ofd_create(const ofd_config *cfg, ofd_handle **out) {
     for (int f = 0; f < NF; ++f) h->s.scale[f] = 1.f;
   for (int i = 0; i < 6; ++i) h->s.face[i] = cfg->free_surface[i];
   h->s.legacy = cfg->legacy_bc;
+  h->s.sr = cfg->rounding == OFD_ROUND_STOCHASTIC ? 1 : 0;
   h->s.dt = cfg->dt;
   for (int i = 0; i < 3; ++i) h->s.h[i] = cfg->spacing[i];
   for (int k = 0; k < 4; ++k) h->s.c[k] = cfg->weights[k];
@@ -449,20 +452,24 @@ int ofd_set_media_const(ofd_handle *h, float beta, float lambda, float mu) {
 
 // Queue the media preprocessing on the handle's stream: rho, vp, vs (host or
 // device memory, dense reference layout) in, the nine effective-media arrays
-// out.  The three inputs pass through one stream-ordered scratch allocation.
+// out.  The three inputs and 1/mu pass through one stream-ordered scratch
+// allocation.
 static int queue_media(ofd_handle *h, const float *rho, const float *vp, const float *vs, cudaMemcpyKind kind) {
   const Geom &g = h->s.g;
   const long n = (long)g.n1 * g.n2 * g.n3;
   float *tmp = nullptr;
-  OFD_CUDA(cudaMallocAsync((void **)&tmp, sizeof(float) * n * 3, h->stream));
+  // three float inputs, then 1/mu in double (8-byte aligned: 3n floats = 12n bytes)
+  OFD_CUDA(cudaMallocAsync((void **)&tmp, sizeof(float) * n * 3 + sizeof(double) * n + 16, h->stream));
+  double *inv_mu = (double *)(((uintptr_t)(tmp + 3 * n) + 15) & ~(uintptr_t)15);
   OFD_CUDA(cudaMemcpyAsync(tmp, rho, sizeof(float) * n, kind, h->stream));
   OFD_CUDA(cudaMemcpyAsync(tmp + n, vp, sizeof(float) * n, kind, h->stream));
   OFD_CUDA(cudaMemcpyAsync(tmp + 2 * n, vs, sizeof(float) * n, kind, h->stream));
   const dim3 blk(32, 8), grd((g.n3 + 31) / 32, (g.n2 + 7) / 8, g.n1);
-  media_fused_kernel<<<grd, blk, 0, h->stream>>>(tmp, tmp + n, tmp + 2 * n, g, h->s.media[M_LAM], h->s.media[M_MU],
-                                                 h->s.media[M_MU12], h->s.media[M_MU13], h->s.media[M_MU23],
-                                                 h->s.media[M_B1], h->s.media[M_B2], h->s.media[M_B3],
-                                                 h->s.media[M_BETA]);
+  media_point_kernel<<<grd, blk, 0, h->stream>>>(tmp, tmp + n, tmp + 2 * n, g, h->s.media[M_BETA],
+                                                 h->s.media[M_LAM], h->s.media[M_MU], inv_mu);
+  media_avg_kernel<<<grd, blk, 0, h->stream>>>(h->s.media[M_BETA], inv_mu, g, h->s.media[M_MU12], h->s.media[M_MU13],
+                                               h->s.media[M_MU23], h->s.media[M_B1], h->s.media[M_B2],
+                                               h->s.media[M_B3]);
   OFD_CUDA(cudaGetLastError());
   OFD_CUDA(cudaFreeAsync(tmp, h->stream));
   return OFD_OK;

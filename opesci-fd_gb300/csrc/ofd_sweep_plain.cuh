@@ -44,13 +44,15 @@ __global__ void __launch_bounds__(256) stress_plain(const __grid_constant__ Swee
   if (z >= g.n3 - g.m || y >= g.n2 - g.m) return;
   const int xb = g.m + blockIdx.z * a.xchunk;
   const int xe = min(xb + a.xchunk, g.n1 - g.m);
+  const long step = a.sr ? *a.step : 0;
   for (int x = xb; x < xe; ++x) {
     const long o = (long)x * g.plane + (long)y * g.P + z;
     PlainAcc<S> A{a, o};
     C out[6];
     GenSweep<R, HET>::template stress<C>(A, (const float *)a.K, out);
 #pragma unroll
-    for (int i = 0; i < 6; ++i) a.out[F_TXX + i][o] = Storage<S>::store(out[i], a.sc[F_TXX + i]);
+    for (int i = 0; i < 6; ++i)
+      a.out[F_TXX + i][o] = SweepStore<S>::st(out[i], a.sc[F_TXX + i], a.sr, a.sr ? sr_hash(o, F_TXX + i, step) : 0u);
   }
 }
 
@@ -63,13 +65,15 @@ __global__ void __launch_bounds__(256) velocity_plain(const __grid_constant__ Sw
   if (z >= g.n3 - g.m || y >= g.n2 - g.m) return;
   const int xb = g.m + blockIdx.z * a.xchunk;
   const int xe = min(xb + a.xchunk, g.n1 - g.m);
+  const long step = a.sr ? *a.step : 0;
   for (int x = xb; x < xe; ++x) {
     const long o = (long)x * g.plane + (long)y * g.P + z;
     PlainAcc<S> A{a, o};
     C out[3];
     GenSweep<R, HET>::template velocity<C>(A, (const float *)a.K, out);
 #pragma unroll
-    for (int i = 0; i < 3; ++i) a.out[F_U + i][o] = Storage<S>::store(out[i], a.sc[F_U + i]);
+    for (int i = 0; i < 3; ++i)
+      a.out[F_U + i][o] = SweepStore<S>::st(out[i], a.sc[F_U + i], a.sr, a.sr ? sr_hash(o, F_U + i, step) : 0u);
   }
 }
 

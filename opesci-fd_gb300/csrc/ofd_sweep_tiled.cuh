@@ -79,6 +79,7 @@ struct TiledParams {
   CUtensorMap pmap[6];     // point boxes of field arrays
   CUtensorMap mmap[5];     // point boxes of media arrays
   CUtensorMap bmap;        // beta boxes (heterogeneous velocity sweep)
+  CUtensorMap xpmap[3];    // point boxes of the x-window arrays (split staging)
   int *err;                // error word (bounded waits)
   unsigned long long wait_ns;   // limit of each pipeline wait (ns of %globaltimer)
   int zcoord0;             // TMA x coordinate of z = m (z0 + m)
@@ -162,15 +163,28 @@ template <typename S, int HET> struct PairMode {
 };
 
 // Compile-time description of one sweep.  Roles of the arrays read:
-//   X  ("x-window"): read at x offsets and with y/z neighbours -> ring of NSH
-//      halo boxes (stress: U V W; velocity: Txx Txy Txz)
-//   H  ("plane halo"): y/z neighbours at the current plane only -> ring of NSC
-//      halo boxes (velocity: Tyy Tyz Tzz)
+//   X  ("x-window"): read at x offsets and with y/z neighbours (stress: U V W;
+//      velocity: Txx Txy Txz)
+//   H  ("plane halo"): y/z neighbours at the current plane only (velocity:
+//      Tyy Tyz Tzz) -> halo boxes in the plane ring
 //   P  (point): the value at the point (stress: the six stresses at t0;
-//      velocity: U V W at t0) and the media arrays -> ring of NSC point boxes
+//      velocity: U V W at t0) and the media arrays -> point boxes in the
+//      plane ring (NSC planes)
+// An X array is staged in one of two ways:
+//   * whole (SPLIT false, space order <= 4): every plane of the x window as a
+//     halo box in the x-window ring (NSH planes);
+//   * split (SPLIT true, space order >= 6): the update reads an X array
+//     either at an x offset (dy = dz = 0) or with a y/z neighbour at the
+//     current plane (dx = 0), never both (the generated expressions mix no
+//     offsets), so the x-window ring holds point boxes only and the current
+//     plane's halo box of each X array read with y/z neighbours goes to the
+//     plane ring.  The halo box re-reads the point values from L2 (they were
+//     fetched R planes earlier); the rings shrink enough to keep two or three
+//     planes in flight (PF), which these orders need to cover DRAM latency.
 template <int R, typename S, int HET, bool STRESS>
 struct TiledCfg {
   static constexpr bool PAIR = PairMode<S, HET>::v;
+  static constexpr bool SPLIT = R >= 3;
   static constexpr int TY = tile_rows(R);
   static constexpr int ZW = PAIR ? 1 : row_warps(R);       // consumer warps per tile row
   static constexpr int NCW = TY * ZW;                      // consumer warps
@@ -179,6 +193,9 @@ struct TiledCfg {
   static constexpr int HW = TZ + 2 * ZH;                   // halo box width
   static constexpr int HH = TY + 2 * R;                    // halo box height
   static constexpr int NXF = 3;                            // x-window arrays
+  // current-plane halo boxes of X arrays (split staging): stress U V W,
+  // velocity Txy Txz (Txx is read at x offsets only)
+  static constexpr int NXH = SPLIT ? (STRESS ? 3 : 2) : 0;
   static constexpr int NH0 = STRESS ? 0 : 3;               // plane-halo arrays
   static constexpr int NPF = STRESS ? 6 : 3;               // point field arrays
   // point media arrays: lambda mu mu12 mu13 mu23 (stress).  The velocity
@@ -188,7 +205,10 @@ struct TiledCfg {
   static constexpr int NMF = (HET && STRESS) ? 5 : 0;
   static constexpr int NBX = (HET && !STRESS) ? 1 : 0;    // beta box per x-window plane
   static constexpr int BW = TZ + 4, BH = TY + 1;          // beta box extent (floats)
-  static constexpr int PF = 1;                             // planes prefetched ahead
+  // planes prefetched ahead: split FP32 staging keeps one CTA per SM with
+  // three planes in flight; 16-bit storage halves the boxes, so two planes in
+  // flight still leave room for two CTAs per SM
+  static constexpr int PF = SPLIT ? (sizeof(S) <= 2 ? 2 : 3) : 1;
   static constexpr int NSH = 2 * R + 1 + PF;               // x-window ring depth
   static constexpr int NSC = 1 + PF;                       // plane ring depth
   static constexpr int HBOX = HW * HH * (int)sizeof(S);
@@ -197,18 +217,20 @@ struct TiledCfg {
   static constexpr int PSLOT = round128(PBOX);
   static constexpr int MBOX = TZ * TY * 4;
   static constexpr int MSLOT = round128(MBOX);
-  // one x-window ring stage holds NXF halo boxes; one plane ring stage holds
-  // NH0 halo boxes, NPF point boxes and NMF media boxes
+  static constexpr int XBOX = SPLIT ? PBOX : HBOX;         // box of an X array in the x-window ring
+  static constexpr int XSLOT = SPLIT ? PSLOT : HSLOT;
+  // one x-window ring stage holds NXF X boxes (+ the beta box); one plane
+  // ring stage holds NXH + NH0 halo boxes, NPF point boxes and NMF media boxes
   static constexpr int BBOX = BW * BH * 4;
   static constexpr int BSLOT = round128(BBOX);
-  static constexpr int XSTAGE = NXF * HSLOT + NBX * BSLOT;
-  static constexpr int CSTAGE = NH0 * HSLOT + NPF * PSLOT + NMF * MSLOT;
+  static constexpr int XSTAGE = NXF * XSLOT + NBX * BSLOT;
+  static constexpr int CSTAGE = (NXH + NH0) * HSLOT + NPF * PSLOT + NMF * MSLOT;
   static constexpr int XRING = NSH * XSTAGE;
   static constexpr int CRING = NSC * CSTAGE;
   static constexpr int BARS = 2 * (NSH + NSC) * 8;        // full and empty barrier per slot
   static constexpr int SMEM = XRING + CRING + round128(BARS) + 128;  // +128: base alignment
-  static constexpr unsigned XBYTES = NXF * HBOX + NBX * BBOX;
-  static constexpr unsigned CBYTES = NH0 * HBOX + NPF * PBOX + NMF * MBOX;
+  static constexpr unsigned XBYTES = NXF * XBOX + NBX * BBOX;
+  static constexpr unsigned CBYTES = (NXH + NH0) * HBOX + NPF * PBOX + NMF * MBOX;
   // role and index of a field id
   __host__ __device__ static constexpr int role(int f) {   // 0 X, 1 H, 2 P
     return STRESS ? (f < F_TXX ? 0 : 2)
@@ -217,13 +239,16 @@ struct TiledCfg {
   __host__ __device__ static constexpr int xidx(int f) {
     return STRESS ? (f - F_U) : (f == F_TXX ? 0 : (f == F_TXY ? 1 : 2));
   }
+  // index among the current-plane halo boxes of X arrays (split staging)
+  __host__ __device__ static constexpr int xhidx(int f) { return STRESS ? (f - F_U) : (f == F_TXY ? 0 : 1); }
   __host__ __device__ static constexpr int h0idx(int f) { return f == F_TYY ? 0 : (f == F_TYZ ? 1 : 2); }
   __host__ __device__ static constexpr int pidx(int f) { return STRESS ? (f - F_TXX) : (f - F_U); }
   __host__ __device__ static constexpr int midx(int m) { return STRESS ? (m - M_LAM) : (m - M_B1); }
   // byte offset of a box inside a plane-ring stage
-  __host__ __device__ static constexpr int h0off(int i) { return i * HSLOT; }
-  __host__ __device__ static constexpr int poff(int i) { return NH0 * HSLOT + i * PSLOT; }
-  __host__ __device__ static constexpr int moff(int i) { return NH0 * HSLOT + NPF * PSLOT + i * MSLOT; }
+  __host__ __device__ static constexpr int xhoff(int i) { return i * HSLOT; }
+  __host__ __device__ static constexpr int h0off(int i) { return (NXH + i) * HSLOT; }
+  __host__ __device__ static constexpr int poff(int i) { return (NXH + NH0) * HSLOT + i * PSLOT; }
+  __host__ __device__ static constexpr int moff(int i) { return (NXH + NH0) * HSLOT + NPF * PSLOT + i * MSLOT; }
 };
 
 // Accessor of the generated expressions: xs[k] is the x-window stage of plane
@@ -241,7 +266,15 @@ struct TiledAcc {
   __device__ __forceinline__ C operator()(int f, int dx, int dy, int dz) const {
     const int off = dy * G::HW + dz;
     if (G::role(f) == 0) {
-      const S *b = (const S *)(xs[dx + R] + G::xidx(f) * G::HSLOT);
+      if (G::SPLIT && dy == 0 && dz == 0) {
+        const S *b = (const S *)(xs[dx + R] + G::xidx(f) * G::XSLOT);
+        return (C)Storage<S>::load(b[ppos], inv[f]);
+      }
+      if (G::SPLIT) {
+        const S *b = (const S *)(cs + G::xhoff(G::xhidx(f)));
+        return (C)Storage<S>::load(b[hpos + off], inv[f]);
+      }
+      const S *b = (const S *)(xs[dx + R] + G::xidx(f) * G::XSLOT);
       return (C)Storage<S>::load(b[hpos + off], inv[f]);
     }
     if (G::role(f) == 1) {
@@ -253,11 +286,11 @@ struct TiledAcc {
   }
   __device__ __forceinline__ C m(int i) const {
     if constexpr (G::NBX != 0) {
-      // beta1..3 = (beta + beta at x+1 / y+1 / z+1) * 0.5f, as media_fused_kernel
-      const float *b = (const float *)(xs[R] + G::NXF * G::HSLOT);
+      // beta1..3 = (beta + beta at x+1 / y+1 / z+1) * 0.5f, as media_avg_kernel
+      const float *b = (const float *)(xs[R] + G::NXF * G::XSLOT);
       const float b0 = b[bpos];
       float b1;
-      if (i == M_B1) b1 = ((const float *)(xs[R + 1] + G::NXF * G::HSLOT))[bpos];
+      if (i == M_B1) b1 = ((const float *)(xs[R + 1] + G::NXF * G::XSLOT))[bpos];
       else if (i == M_B2) b1 = b[bpos + G::BW];
       else b1 = b[bpos + 1];
       return (C)((b0 + b1) * 0.5f);
@@ -282,8 +315,14 @@ struct TiledAcc2 {
   __device__ __forceinline__ F2 operator()(int f, int dx, int dy, int dz) const {
     const S *b;
     int pos;
-    if (G::role(f) == 0) {
-      b = (const S *)(xs[dx + R] + G::xidx(f) * G::HSLOT);
+    if (G::role(f) == 0 && G::SPLIT && dy == 0 && dz == 0) {
+      b = (const S *)(xs[dx + R] + G::xidx(f) * G::XSLOT);
+      pos = ppos;
+    } else if (G::role(f) == 0 && G::SPLIT) {
+      b = (const S *)(cs + G::xhoff(G::xhidx(f)));
+      pos = hpos + dy * G::HW + dz;
+    } else if (G::role(f) == 0) {
+      b = (const S *)(xs[dx + R] + G::xidx(f) * G::XSLOT);
       pos = hpos + dy * G::HW + dz;
     } else if (G::role(f) == 1) {
       b = (const S *)(cs + G::h0off(G::h0idx(f)));
@@ -297,11 +336,11 @@ struct TiledAcc2 {
   }
   __device__ __forceinline__ F2 m(int i) const {
     if constexpr (G::NBX != 0) {
-      // beta1..3 = (beta + beta at x+1 / y+1 / z+1) * 0.5f, as media_fused_kernel
-      const float *b = (const float *)(xs[R] + G::NXF * G::HSLOT);
+      // beta1..3 = (beta + beta at x+1 / y+1 / z+1) * 0.5f, as media_avg_kernel
+      const float *b = (const float *)(xs[R] + G::NXF * G::XSLOT);
       const F2 b0 = PairLoad<float, true>::ld(b + bpos, 1.f, nz);
       F2 b1;
-      if (i == M_B1) b1 = PairLoad<float, true>::ld((const float *)(xs[R + 1] + G::NXF * G::HSLOT) + bpos, 1.f, nz);
+      if (i == M_B1) b1 = PairLoad<float, true>::ld((const float *)(xs[R + 1] + G::NXF * G::XSLOT) + bpos, 1.f, nz);
       else if (i == M_B2) b1 = PairLoad<float, true>::ld(b + bpos + G::BW, 1.f, nz);
       else b1 = PairLoad<float, false>::ld(b + bpos + 1, 1.f, nz);
       // the sum is rounded, then halved (a product of a sum: nothing to fuse)
@@ -314,13 +353,13 @@ struct TiledAcc2 {
 
 // Launch shape of a tiled sweep: 32 threads per consumer warp plus the
 // producer warp, and the resident CTAs per SM the register budget is sized
-// for.  Space order >= 6 keeps one CTA per SM (its rings fill shared memory),
-// so ptxas may use the whole register file rather than spill; the paired
-// evaluation at lower orders keeps two CTAs per SM.
+// for.  Space order >= 6 with FP32 storage keeps one CTA per SM (its rings
+// fill shared memory), so ptxas may use the whole register file rather than
+// spill; lower orders and paired 16-bit storage keep two CTAs per SM.
 template <int R, typename S, int HET> struct TiledLaunch {
   static constexpr int ZW = PairMode<S, HET>::v ? 1 : row_warps(R);
   static constexpr int THREADS = 32 * (tile_rows(R) * ZW + 1);
-  static constexpr int MIN_BLOCKS = R >= 3 ? 1 : (PairMode<S, HET>::v ? 2 : 0);
+  static constexpr int MIN_BLOCKS = R >= 3 ? ((PairMode<S, HET>::v && sizeof(S) == 2) ? 2 : 1) : 2;
 };
 
 // The literal table of a heterogeneous expression held as its few distinct
@@ -385,14 +424,22 @@ __device__ __forceinline__ void sweep_tile(const SweepArgs<S> &a, const TiledPar
     mbar_expect_tx(bar, G::XBYTES);
     unsigned char *st = xring + slot * G::XSTAGE;
 #pragma unroll
-    for (int i = 0; i < G::NXF; ++i) tma_load_3d(st + i * G::HSLOT, &p.hmap[i], bar, zc - G::ZH, y0 - R, plane);
-    if constexpr (G::NBX != 0) tma_load_3d(st + G::NXF * G::HSLOT, &p.bmap, bar, zc, y0, plane);
+    for (int i = 0; i < G::NXF; ++i) {
+      if constexpr (G::SPLIT) tma_load_3d(st + i * G::XSLOT, &p.xpmap[i], bar, zc, y0, plane);
+      else tma_load_3d(st + i * G::XSLOT, &p.hmap[i], bar, zc - G::ZH, y0 - R, plane);
+    }
+    if constexpr (G::NBX != 0) tma_load_3d(st + G::NXF * G::XSLOT, &p.bmap, bar, zc, y0, plane);
   };
   auto issue_c = [&](int plane) {
     const int slot = (plane - xb) % G::NSC;
     uint64_t *bar = &cbar[slot];
     mbar_expect_tx(bar, G::CBYTES);
     unsigned char *st = cring + slot * G::CSTAGE;
+    // current-plane halo boxes of the X arrays read with y/z neighbours
+    // (split staging): stress U V W = hmap[0..2], velocity Txy Txz = hmap[1..2]
+#pragma unroll
+    for (int i = 0; i < G::NXH; ++i)
+      tma_load_3d(st + G::xhoff(i), &p.hmap[STRESS ? i : i + 1], bar, zc - G::ZH, y0 - R, plane);
 #pragma unroll
     for (int i = 0; i < G::NH0; ++i) tma_load_3d(st + G::h0off(i), &p.hmap[G::NXF + i], bar, zc - G::ZH, y0 - R, plane);
 #pragma unroll
@@ -446,6 +493,7 @@ __device__ __forceinline__ void sweep_tile(const SweepArgs<S> &a, const TiledPar
   } else {
     const int yl = warp / G::ZW, zpart = warp % G::ZW;
     const int y = y0 + yl;
+    const long step = a.sr ? *a.step : 0;   // rounding hash of 16-bit stores
     int hwaited = hq0 - 1;   // last x-window plane waited for
     for (int x = xb; x < xe; ++x) {
       bool ok = true;
@@ -487,14 +535,16 @@ __device__ __forceinline__ void sweep_tile(const SweepArgs<S> &a, const TiledPar
           GenSweep<R, HET>::template stress<F2>(A, K, out);
           if (in0) {
 #pragma unroll
-            for (int i = 0; i < 6; ++i) PairStore<S>::st(a.out[F_TXX + i] + o, out[i], a.sc[F_TXX + i], in1);
+            for (int i = 0; i < 6; ++i)
+              PairStore<S>::st(a.out[F_TXX + i] + o, out[i], a.sc[F_TXX + i], in1, a.sr, o, F_TXX + i, step);
           }
         } else {
           F2 out[3];
           GenSweep<R, HET>::template velocity<F2>(A, K, out);
           if (in0) {
 #pragma unroll
-            for (int i = 0; i < 3; ++i) PairStore<S>::st(a.out[F_U + i] + o, out[i], a.sc[F_U + i], in1);
+            for (int i = 0; i < 3; ++i)
+              PairStore<S>::st(a.out[F_U + i] + o, out[i], a.sc[F_U + i], in1, a.sr, o, F_U + i, step);
           }
         }
       } else {
@@ -517,14 +567,18 @@ __device__ __forceinline__ void sweep_tile(const SweepArgs<S> &a, const TiledPar
             GenSweep<R, HET>::template stress<C>(A, K, out);
             if (inside) {
 #pragma unroll
-              for (int i = 0; i < 6; ++i) a.out[F_TXX + i][o] = Storage<S>::store(out[i], a.sc[F_TXX + i]);
+              for (int i = 0; i < 6; ++i)
+                a.out[F_TXX + i][o] =
+                    SweepStore<S>::st(out[i], a.sc[F_TXX + i], a.sr, a.sr ? sr_hash(o, F_TXX + i, step) : 0u);
             }
           } else {
             C out[3];
             GenSweep<R, HET>::template velocity<C>(A, K, out);
             if (inside) {
 #pragma unroll
-              for (int i = 0; i < 3; ++i) a.out[F_U + i][o] = Storage<S>::store(out[i], a.sc[F_U + i]);
+              for (int i = 0; i < 3; ++i)
+                a.out[F_U + i][o] =
+                    SweepStore<S>::st(out[i], a.sc[F_U + i], a.sr, a.sr ? sr_hash(o, F_U + i, step) : 0u);
             }
           }
         }
@@ -626,6 +680,11 @@ sweep_tiled_group(const GroupSweep<S> *__restrict__ tab, int n) {
     for (int i = 0; i < G::NMF; ++i)
       asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(&e.p.mmap[i]) : "memory");
     if (G::NBX) asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(&e.p.bmap) : "memory");
+    if (G::SPLIT) {
+#pragma unroll 1
+      for (int i = 0; i < G::NXF; ++i)
+        asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(&e.p.xpmap[i]) : "memory");
+    }
   }
   const int local = (int)blockIdx.x - e.cta_begin;
   if constexpr (KD && PairMode<S, HET>::v) {
@@ -674,12 +733,14 @@ void tiled_params(const SweepArgs<S> &a, const TiledCtx &ctx, int t0, int chunk_
   const int t1 = 1 - t0;
   if (STRESS) {
     for (int i = 0; i < 3; ++i) p.hmap[i] = mp->halo[F_U + i][t0];
+    for (int i = 0; i < 3; ++i) p.xpmap[i] = mp->point[F_U + i][t0];
     for (int i = 0; i < 6; ++i) p.pmap[i] = mp->point[F_TXX + i][t0];
     for (int i = 0; i < 5; ++i) p.mmap[i] = mp->media[M_LAM + i];
   } else {
     // x-window arrays first (Txx Txy Txz), then plane-halo arrays (Tyy Tyz Tzz)
     const int order[6] = {F_TXX, F_TXY, F_TXZ, F_TYY, F_TYZ, F_TZZ};
     for (int i = 0; i < 6; ++i) p.hmap[i] = mp->halo[order[i]][t1];
+    for (int i = 0; i < 3; ++i) p.xpmap[i] = mp->point[order[i]][t1];
     for (int i = 0; i < 3; ++i) p.pmap[i] = mp->point[F_U + i][t0];
     if (G::NBX) p.bmap = mp->beta;
   }

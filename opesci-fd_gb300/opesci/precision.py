@@ -9,7 +9,9 @@ scaling itself is exact and only the 16-bit rounding remains.
     python -m opesci.precision study --size 768 --space-order 8 --steps 800
     python -m opesci.precision convergence --sizes 64 128 256
 
-print one JSON object each.
+print one JSON object each (run from opesci-fd_gb300/, or with it on
+PYTHONPATH).  Storage names: f64, f32, f16, bf16, and f16sr / bf16sr for the
+16-bit types with stochastic rounding of the sweeps' stores.
 """
 import argparse
 import json
@@ -25,9 +27,17 @@ FP16_MAX = 65504.0
 FIELDS = runtime.FIELDS
 
 
+def split_storage(name):
+    """'f16sr' / 'bf16sr' -> (storage, 'stochastic'); others -> (name, 'nearest')."""
+    if name.endswith('sr'):
+        return name[:-2], 'stochastic'
+    return name, 'nearest'
+
+
 def choose_scales(absmax, storage, headroom=8.0):
     """Per-field power-of-two scales: FP16 keeps max|f| * scale within
     65504/headroom (largest such power of two); BF16, FP32 and FP64 use 1."""
+    storage = split_storage(storage)[0]
     if storage not in ('f16', 'fp16', 'half'):
         return [1.0] * 9
     out = []
@@ -41,7 +51,8 @@ def choose_scales(absmax, storage, headroom=8.0):
 
 
 def _problem_sim(grid, media, src, wav, storage, scales=None):
-    cfg = runtime.config_from_grid(grid, storage=storage, field_scale=scales)
+    st, rounding = split_storage(storage)
+    cfg = runtime.config_from_grid(grid, storage=st, field_scale=scales, rounding=rounding)
     sim = runtime.Simulation(cfg)
     sim.set_coefficients_from_grid(grid)
     sim.set_media(*media)
@@ -49,7 +60,7 @@ def _problem_sim(grid, media, src, wav, storage, scales=None):
     return sim
 
 
-def precision_study(n=128, space_order=8, steps=200, seed=0, storages=('f32', 'f16', 'bf16'),
+def precision_study(n=128, space_order=8, steps=200, seed=0, storages=('f32', 'f16', 'bf16', 'f16sr', 'bf16sr'),
                     checkpoints=8):
     """Config-3 style study on an n^3 layered problem: returns, per storage,
     the per-field relative L2 error of the final state against an FP64 run,
@@ -96,7 +107,8 @@ def eigen_errors(n, storage, tmax=0.25, c=4.096, space_order=4):
     g = eigenwave_grid(grid_size=(n, n, n), dt=dt, ntsteps=steps, space_order=space_order)
     A = math.sqrt(2 * g.defined_variable['mu'].value / g.defined_variable['beta'].value)
     scales = choose_scales([2.0] * 3 + [2.0 * A] * 6, storage)
-    sim = runtime.Simulation(runtime.config_from_grid(g, storage=storage, field_scale=scales))
+    st, rounding = split_storage(storage)
+    sim = runtime.Simulation(runtime.config_from_grid(g, storage=st, field_scale=scales, rounding=rounding))
     sim.set_coefficients_from_grid(g)
     dv = g.defined_variable
     sim.set_media_const(dv['beta'].value, dv['lambda'].value, dv['mu'].value)
@@ -110,7 +122,8 @@ def eigen_errors(n, storage, tmax=0.25, c=4.096, space_order=4):
     return {'n': n, 'dt': dt, 'steps': steps, 'l2': errs}
 
 
-def convergence_study(sizes=(64, 128, 256), storages=('f64', 'f32', 'f16', 'bf16'), tmax=0.25, c=4.096):
+def convergence_study(sizes=(64, 128, 256), storages=('f64', 'f32', 'f16', 'bf16', 'f16sr', 'bf16sr'), tmax=0.25,
+                      c=4.096):
     """Errors and observed orders log2(e_h / e_h/2) per storage and field."""
     out = {'sizes': list(sizes), 'tmax': tmax, 'c': c, 'runs': {}}
     for st in storages:

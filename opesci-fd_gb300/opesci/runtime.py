@@ -34,7 +34,8 @@ class ofd_config(ctypes.Structure):
                 ('dt', ctypes.c_double),
                 ('weights', ctypes.c_double * 4),
                 ('field_scale', ctypes.c_float * 9),
-                ('kernel_variant', ctypes.c_int)]
+                ('kernel_variant', ctypes.c_int),
+                ('rounding', ctypes.c_int)]
 
 
 REGULAR_MAX_TERMS = 96
@@ -167,8 +168,11 @@ def _fptr(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
 
 
+ROUNDING = {'nearest': 0, 'stochastic': 1}
+
+
 def make_config(dims, space_order, spacing, dt, weights, storage='f32', free_surface=None,
-                legacy_bc=False, field_scale=None, kernel_variant=0):
+                legacy_bc=False, field_scale=None, kernel_variant=0, rounding='nearest'):
     cfg = ofd_config()
     for i in range(3):
         cfg.dim[i] = int(dims[i])
@@ -186,10 +190,11 @@ def make_config(dims, space_order, spacing, dt, weights, storage='f32', free_sur
     for f in range(9):
         cfg.field_scale[f] = float(field_scale[f]) if field_scale is not None else 1.0
     cfg.kernel_variant = int(kernel_variant)
+    cfg.rounding = ROUNDING[rounding] if isinstance(rounding, str) else int(rounding)
     return cfg
 
 
-def config_from_grid(grid, storage=None, kernel_variant=0, field_scale=None):
+def config_from_grid(grid, storage=None, kernel_variant=0, field_scale=None, rounding='nearest'):
     """ofd_config of a solved StaggeredGrid: dims, margin, spacing, dt, the
     staggered weights of its space order, per-face free-surface algorithms."""
     faces = [0] * 6
@@ -201,7 +206,7 @@ def config_from_grid(grid, storage=None, kernel_variant=0, field_scale=None):
     return make_config([d.value for d in grid.dim], grid.order[1], [s.value for s in grid.spacing],
                        grid.dt.value, grid.fd_weights(), storage=storage, free_surface=faces,
                        legacy_bc=getattr(grid, 'legacy_bc', False), field_scale=field_scale,
-                       kernel_variant=kernel_variant)
+                       kernel_variant=kernel_variant, rounding=rounding)
 
 
 class Simulation(object):

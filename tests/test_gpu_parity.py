@@ -142,13 +142,17 @@ FACE_MIXES = {
 def run_random_state(so, n, faces, storage, mode, steps=6):
     """Layered media, random initial fields everywhere (so every ghost and
     recompute path sees non-zero data), ``steps`` steps.  mode: 'tiled',
-    'plain' (kernel variant 1) or 'persistent'."""
+    'plain' (kernel variant 1) or 'persistent'.  A storage name ending in
+    'sr' selects stochastic rounding of the 16-bit stores."""
     from opesci.batch import Shot
     cfg, media, src, wav, ks, kv = Shot(n, so, steps, 21, 12.0).build()
+    rounding = 'stochastic' if storage.endswith('sr') else 'nearest'
+    storage = storage[:-2] if storage.endswith('sr') else storage
     # velocities ~1e-7 m/s and stresses ~1 Pa, as in the layered problems
     scales = [2.0 ** 30] * 3 + [2.0 ** 9] * 6 if storage in ('f16', 'bf16') else None
     c = runtime.make_config(list(cfg.dim), so, list(cfg.spacing), cfg.dt, list(cfg.weights), storage=storage,
-                            free_surface=faces, field_scale=scales, kernel_variant=1 if mode == 'plain' else 0)
+                            free_surface=faces, field_scale=scales, kernel_variant=1 if mode == 'plain' else 0,
+                            rounding=rounding)
     sim = runtime.Simulation(c)
     sim.set_coefficients(1, ks, kv)
     sim.set_media(*media)
@@ -174,6 +178,8 @@ def run_random_state(so, n, faces, storage, mode, steps=6):
     (4, 72, 'levander', 'f32'), (4, 70, 'mixed', 'f32'), (4, 66, 'zfree', 'f32'), (4, 72, 'levander', 'f16'),
     (8, 68, 'robertsson', 'f32'), (6, 67, 'mixed', 'f32'), (2, 70, 'robertsson', 'f32'),
     (8, 66, 'robertsson', 'bf16'),
+    # stochastic rounding of the 16-bit stores (same hash on every path)
+    (4, 72, 'levander', 'f16sr'), (8, 66, 'mixed', 'bf16sr'), (6, 67, 'robertsson', 'f16sr'),
     # four z tiles
     (4, 200, 'levander', 'f32'), (8, 196, 'mixed', 'f32'), (4, 193, 'zfree', 'f16')])
 def test_boundary_paths_identical_across_kernels(so, n, faces, storage):
