@@ -20,7 +20,11 @@
  *  - field numbers follow the reference's OpesciGrid order, velocities then
  *    stresses (staggeredgrid.py:69-71): U V W Txx Tyy Tzz Txy Tyz Txz;
  *  - one CUDA stream per handle; calls on one handle are not re-entrant,
- *    different handles are independent.
+ *    different handles are independent;
+ *  - transient device scratch (media preprocessing, transfers of 16-bit and
+ *    FP64 fields) comes from a stream-ordered pool of the library, one per
+ *    device, which keeps up to 4 GiB mapped between calls; ofd_footprint
+ *    does not count it.
  */
 #ifndef OFD_H
 #define OFD_H
@@ -109,6 +113,15 @@ int ofd_set_media_async(ofd_handle *h, const float *rho, const float *vp, const 
  * constant media folded into the literals.  nks/nkv must equal the table
  * sizes of the prebuilt expression for this space order and media mode. */
 int ofd_set_coefficients(ofd_handle *h, int het, const float *ks, int nks, const float *kv, int nkv);
+/* Literal table of the generated space-order-4 Levander ghost expressions
+ * (the frontend's ghost equations fields.py:192-381 as staggeredgrid.py:754-864
+ * applies them, printed like the update expressions; values as
+ * opesci.templates.cuda_gen.ghost_table computes them).  With it the ghost
+ * cells are evaluated from those printed expressions, term for term; without
+ * it (or nkg = 0) from restated formulas that agree to rounding.  Needs
+ * space order 4, Levander free surfaces on all six faces, FP32/FP16/BF16
+ * storage and ofd_set_coefficients of the same media mode first. */
+int ofd_set_ghost_coefficients(ofd_handle *h, int het, const float *kg, int nkg);
 
 /* Field transfer, reference layout, host memory (pageable or pinned); the
  * calls return once the copy is complete.  The reference publishes its host

@@ -32,8 +32,16 @@
 //    lower v_j[b-1] = v_j[b] + G(b-1) - (mu_hi/mu_lo)(v_j[b+1] - v_j[b] + G(b)),
 //    upper v_j[b+1] = v_j[b] - G(b) + (mu_lo/mu_hi)(v_j[b] - v_j[b-1] + G(b-1));
 //  * Robertsson: R ghost layers set to zero (fields.py:243-259).
+//
+// Space order 4 with the generated ghost expressions (BcArgs::gen): the
+// recomputed normal stresses and the Levander velocity ghosts are the
+// frontend's own printed ghost equations (generated/ghosts_gen.cuh), term for
+// term, which makes the ghost values bit for bit those of the reference's C.
+// The formulas above stay as the path for FP64 storage and for models whose
+// ghost equations have another structure.
 #pragma once
 #include "ofd_common.cuh"
+#include "generated/ghosts_gen.cuh"
 
 namespace ofd {
 
@@ -67,6 +75,46 @@ __device__ __forceinline__ int mu_pair(int a, int b) {
   if (lo == 0 && hi == 1) return M_MU12;
   if (lo == 0 && hi == 2) return M_MU13;
   return M_MU23;
+}
+
+// Accessor of the generated ghost expressions: A(F, level, ox, oy, oz) is
+// field F at level t0 (0) or t1 (1) at an offset from the point o on the
+// boundary plane, A.m(M, ox, oy, oz) a medium there.  For the tangential
+// velocity ghosts, the along-d component's ghost at this point (offset go)
+// and at the next point along axis ja is the fresh value (v0, vn) the same
+// launch computes, as the reference's face order has written it by then.
+template <typename S, bool COH>
+struct GhostAcc {
+  const BcArgs<S> &a;
+  long o;
+  int fd;          // field whose fresh ghost values are used (-1: none)
+  int go[3];       // offset of that ghost at this point
+  int ja;          // axis of the neighbour holding vn
+  float v0, vn;
+  __device__ __forceinline__ float operator()(int f, int lvl, int ox, int oy, int oz) const {
+    if (f == fd) {
+      const int e[3] = {ox - go[0], oy - go[1], oz - go[2]};
+      if (e[0] == 0 && e[1] == 0 && e[2] == 0) return v0;
+      if (e[ja] == 1 && e[(ja + 1) % 3] == 0 && e[(ja + 2) % 3] == 0) return vn;
+    }
+    const S *p = lvl ? (const S *)a.f1[f] : a.f0[f];
+    return (float)Storage<S>::load(ldg<COH>(&p[o + ox * a.g.plane + oy * a.g.P + oz]), a.inv[f]);
+  }
+  __device__ __forceinline__ float m(int i, int ox, int oy, int oz) const {
+    return a.media[i][o + ox * a.g.plane + oy * a.g.P + oz];
+  }
+};
+
+template <typename S, bool COH>
+__device__ __forceinline__ GhostAcc<S, COH> ghost_acc(const BcArgs<S> &a, long o) {
+  return GhostAcc<S, COH>{a, o, -1, {0, 0, 0}, 0, 0.f, 0.f};
+}
+
+// generated velocity ghost of component c on face (d, side) at point o of
+// the boundary plane, through accessor A
+template <class Acc, class S>
+__device__ __forceinline__ float gen_velocity_ghost(const BcArgs<S> &a, int c, int d, int side, const Acc &A) {
+  return a.het ? GenGhost4<1>::velocity(c, d, side, A, a.kg) : GenGhost4<0>::velocity(c, d, side, A, a.kg);
 }
 
 // Stress ghosts of face normal d at in-plane point (i1, i2) for stress
@@ -116,6 +164,15 @@ __device__ __forceinline__ void stress_bc_point(const BcArgs<S> &a, int d, int i
   if (!normal || fb != 1 || !a.recompute) return;
   if (i1 < m + 1 || i1 >= n1 - m - 1 || i2 < m + 1 || i2 >= n2 - m - 1) return;
   // Levander recompute of T_aa (a = dA) on plane b
+  if constexpr (R == 2 && sizeof(S) <= 4) {
+    if (a.gen) {
+      const long o = base + b * sd;
+      const auto A = ghost_acc<S, COH>(a, o);
+      const float v = a.het ? GenGhost4<1>::stress(fi, d, side, A, a.kg) : GenGhost4<0>::stress(fi, d, side, A, a.kg);
+      T[o] = Storage<S>::store(v, a.sc[F]);
+      return;
+    }
+  }
   const int ax = dA;
   const int e = 3 - ax - d;
   const long o = base + b * sd;
@@ -272,6 +329,36 @@ __device__ __forceinline__ void velocity_bc_merged_point(const BcArgs<S> &a, int
     const long base = lin(g, c[0], c[1], c[2]);
     const long ob = base + b * sd, obm = ob - sd;
     const long gpos = side == 0 ? obm : ob;        // where the along-d ghost lives
+    if constexpr (R == 2 && sizeof(S) <= 4) {
+      if (a.gen) {
+        // the generated ghost expressions; offsets are taken from plane b
+        const float vg = gen_velocity_ghost(a, d, d, side, ghost_acc<S, COH>(a, ob));
+        a.f1[Fd][gpos] = Storage<S>::store(vg, a.sc[Fd]);
+        const float vg0 = Storage<S>::load(Storage<S>::store(vg, a.sc[Fd]), a.inv[Fd]);
+        for (int t = 0; t < 2; ++t) {
+          const int j = t == 0 ? a1 : a2;
+          const long sj = gstride(g, j);
+          // along-d ghost at the next point along j: recomputed where the
+          // reference's face order has written it first, else the stored value
+          const int n1j = t == 0 ? i1 + 1 : i1, n2j = t == 0 ? i2 : i2 + 1;
+          const bool in = n1j >= 1 && n1j < n1 - 1 && n2j >= 1 && n2j < n2 - 1;
+          const float vgn =
+              in ? Storage<S>::load(Storage<S>::store(gen_velocity_ghost(a, d, d, side, ghost_acc<S, COH>(a, ob + sj)),
+                                                      a.sc[Fd]), a.inv[Fd])
+                 : (float)Storage<S>::load(ldg<COH>(&a.f1[Fd][gpos + sj]), a.inv[Fd]);
+          GhostAcc<S, COH> A = ghost_acc<S, COH>(a, ob);
+          A.fd = Fd;
+          A.go[d] = side == 0 ? -1 : 0;
+          A.ja = j;
+          A.v0 = vg0;
+          A.vn = vgn;
+          const int F = F_U + j;
+          const float val = gen_velocity_ghost(a, j, d, side, A);
+          a.f1[F][side == 0 ? obm : ob + sd] = Storage<S>::store(val, a.sc[F]);
+        }
+        continue;
+      }
+    }
     const C vg = levander_normal_ghost<S, COH>(a, d, side, i1, i2);
     a.f1[Fd][gpos] = Storage<S>::store(vg, a.sc[Fd]);
     auto LD = [&](int f, long off) -> C { return Storage<S>::load(ldg<COH>(&a.f1[f][off]), a.inv[f]); };

@@ -153,6 +153,11 @@ template <typename S> struct BcArgs {
   int sub;             // velocity: 0 = component along d, 1 = the other two
   typename Storage<S>::C dt, h[3];
   typename Storage<S>::C c4[2];  // 4th-order weights 9/8, -1/24
+  // space order 4, Levander faces: evaluate the generated ghost expressions
+  // (GenGhost4<het>, literals kg in device memory) instead of the restated
+  // formulas
+  int gen, het;
+  const float *kg;
 };
 
 }  // namespace ofd

@@ -45,6 +45,8 @@ struct DevState {
   unsigned *d_bar;     // grid-barrier words of the persistent kernel
   int het;             // 1: media arrays are factors of the update (read mode)
   int sr;              // 16-bit storage: stochastic rounding of the sweeps' stores
+  int gen_ghost;       // space order 4: generated Levander ghost expressions (literals d_kg)
+  float *d_kg;
   int nks, nkv;        // literal-table sizes (0 until ofd_set_coefficients)
   float Ks[OFD_MAX_K], Kv[OFD_MAX_K];
 };
@@ -77,6 +79,9 @@ struct Backend {
   virtual int step_persistent(const DevState &s, int p0, int nsteps, cudaStream_t st) = 0;
   // literal-table sizes of the generated expressions for media mode het
   virtual int table_size(int het, int stress) const = 0;
+  // literal-table size of the generated ghost expressions (0: none for this
+  // space order and storage)
+  virtual int ghost_table_size(int het) const = 0;
   // Grouped stepping: device tables of the members' arguments (all members
   // share this backend's space order and storage, and one media mode), and
   // one step of every member in 8 grouped launches.  chunk_planes: x chunk
@@ -255,6 +260,9 @@ struct Impl : Backend {
     a.c4[1] = (C)(-1.0 / 24.0);
     a.d = 0;
     a.sub = 0;
+    a.gen = (R == 2 && sizeof(S) <= 4 && s.gen_ghost && s.d_kg) ? 1 : 0;
+    a.het = s.het;
+    a.kg = s.d_kg;
     return a;
   }
 
@@ -623,6 +631,11 @@ struct Impl : Backend {
   bool kmap_ok(const DevState &s, bool stress) const override {
     const DevState *m[1] = {&s};
     return stress ? tables_follow_kmap<true>(m, 1) : tables_follow_kmap<false>(m, 1);
+  }
+
+  int ghost_table_size(int het) const override {
+    if constexpr (R == 2 && sizeof(S) <= 4) return het ? GenGhost4<1>::NK : GenGhost4<0>::NK;
+    return 0;
   }
 
   int table_size(int het, int stress) const override {

@@ -89,6 +89,42 @@ __global__ void media_avg_kernel(const float *o_beta_in, const double *__restric
   o_mu23[o] = (float)(1.0 / (0.25 * (m0 + my + mz + im[D(x, y1, z1)])));
 }
 
+// Library-owned stream-ordered pool for transient device scratch (media
+// preprocessing, transfers of non-FP32 fields), one per device.  It keeps up
+// to SCRATCH_KEEP bytes mapped between calls, so repeated jobs (serving,
+// batching) do not map and unmap gigabytes per call; the device's default
+// pool, which other libraries share, is left as it is.
+constexpr unsigned long long SCRATCH_KEEP = 4ULL << 30;
+
+cudaError_t scratch_alloc(void **p, size_t bytes, cudaStream_t st) {
+  static std::mutex mu;
+  static cudaMemPool_t pools[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaMallocAsync(p, bytes, st);
+  cudaMemPool_t pool;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    if (!pools[dev]) {
+      cudaMemPoolProps props = {};
+      props.allocType = cudaMemAllocationTypePinned;
+      props.handleTypes = cudaMemHandleTypeNone;
+      props.location.type = cudaMemLocationTypeDevice;
+      props.location.id = dev;
+      e = cudaMemPoolCreate(&pools[dev], &props);
+      if (e != cudaSuccess) {
+        pools[dev] = nullptr;
+        return e;
+      }
+      unsigned long long keep = SCRATCH_KEEP;
+      cudaMemPoolSetAttribute(pools[dev], cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    pool = pools[dev];
+  }
+  return cudaMallocFromPoolAsync(p, bytes, pool, st);
+}
+
 __global__ void fill_kernel(float *p, long n, float v) {
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) p[i] = v;
 }
@@ -363,6 +399,8 @@ int ofd_create(const ofd_config *cfg, ofd_handle **out) {
   for (int i = 0; i < 6; ++i) h->s.face[i] = cfg->free_surface[i];
   h->s.legacy = cfg->legacy_bc;
   h->s.sr = cfg->rounding == OFD_ROUND_STOCHASTIC ? 1 : 0;
+  h->s.gen_ghost = 0;
+  h->s.d_kg = nullptr;
   h->s.dt = cfg->dt;
   for (int i = 0; i < 3; ++i) h->s.h[i] = cfg->spacing[i];
   for (int k = 0; k < 4; ++k) h->s.c[k] = cfg->weights[k];
@@ -408,6 +446,7 @@ int ofd_destroy(ofd_handle *h) {
   delete h->be;
   delete h->maps;
   if (h->s.d_wav) cudaFree(h->s.d_wav);
+  if (h->s.d_kg) cudaFree(h->s.d_kg);
   if (h->s.d_rec) cudaFree(h->s.d_rec);
   if (h->s.d_traces) cudaFree(h->s.d_traces);
   if (h->fields_raw) cudaFree(h->fields_raw);
@@ -439,6 +478,34 @@ int ofd_set_coefficients(ofd_handle *h, int het, const float *ks, int nks, const
   return OFD_OK;
 }
 
+int ofd_set_ghost_coefficients(ofd_handle *h, int het, const float *kg, int nkg) {
+  if (!h) return fail(OFD_EINVAL, "null handle");
+  if (nkg == 0) {
+    h->s.gen_ghost = 0;
+    drop_graphs(h);
+    return OFD_OK;
+  }
+  if (!kg) return fail(OFD_EINVAL, "null table");
+  if (het != 0 && het != 1) return fail(OFD_EINVAL, "het must be 0 or 1");
+  if (h->s.nks == 0 || het != h->s.het)
+    return fail(OFD_ESTATE, "set the update coefficients of the same media mode first");
+  const int want = h->be->ghost_table_size(het);
+  if (want == 0)
+    return fail(OFD_EINVAL, "no generated ghost expressions for space order %d and this storage", h->cfg.space_order);
+  if (nkg != want)
+    return fail(OFD_EINVAL, "ghost coefficient table of size %d does not match the prebuilt expressions (%d)", nkg, want);
+  for (int i = 0; i < 6; ++i)
+    if (h->cfg.free_surface[i] != OFD_BC_LEVANDER)
+      return fail(OFD_EINVAL, "generated ghost expressions need Levander free surfaces on all six faces");
+  OFD_CUDA(cudaStreamSynchronize(h->stream));
+  if (!h->s.d_kg) OFD_CUDA(cudaMalloc((void **)&h->s.d_kg, sizeof(float) * (size_t)want));
+  OFD_CUDA(cudaMemcpyAsync(h->s.d_kg, kg, sizeof(float) * (size_t)nkg, cudaMemcpyHostToDevice, h->stream));
+  OFD_CUDA(cudaStreamSynchronize(h->stream));
+  h->s.gen_ghost = 1;
+  drop_graphs(h);
+  return OFD_OK;
+}
+
 int ofd_set_media_const(ofd_handle *h, float beta, float lambda, float mu) {
   if (!h) return fail(OFD_EINVAL, "null handle");
   const long n = h->media_elems;
@@ -459,7 +526,7 @@ static int queue_media(ofd_handle *h, const float *rho, const float *vp, const f
   const long n = (long)g.n1 * g.n2 * g.n3;
   float *tmp = nullptr;
   // three float inputs, then 1/mu in double (8-byte aligned: 3n floats = 12n bytes)
-  OFD_CUDA(cudaMallocAsync((void **)&tmp, sizeof(float) * n * 3 + sizeof(double) * n + 16, h->stream));
+  OFD_CUDA(scratch_alloc((void **)&tmp, sizeof(float) * n * 3 + sizeof(double) * n + 16, h->stream));
   double *inv_mu = (double *)(((uintptr_t)(tmp + 3 * n) + 15) & ~(uintptr_t)15);
   OFD_CUDA(cudaMemcpyAsync(tmp, rho, sizeof(float) * n, kind, h->stream));
   OFD_CUDA(cudaMemcpyAsync(tmp + n, vp, sizeof(float) * n, kind, h->stream));
@@ -525,7 +592,7 @@ static int queue_upload(ofd_handle *h, int field, int level, const float *host) 
   }
   const long n = (long)g.n1 * g.n2 * g.n3;
   float *tmp = nullptr;
-  OFD_CUDA(cudaMallocAsync((void **)&tmp, sizeof(float) * n, h->stream));
+  OFD_CUDA(scratch_alloc((void **)&tmp, sizeof(float) * n, h->stream));
   OFD_CUDA(cudaMemcpyAsync(tmp, host, sizeof(float) * n, cudaMemcpyDefault, h->stream));
   h->be->to_padded(h->s, tmp, field, level, h->stream);
   OFD_CUDA(cudaGetLastError());
@@ -543,7 +610,7 @@ static int queue_download(ofd_handle *h, int field, int level, float *host) {
   }
   const long n = (long)g.n1 * g.n2 * g.n3;
   float *tmp = nullptr;
-  OFD_CUDA(cudaMallocAsync((void **)&tmp, sizeof(float) * n, h->stream));
+  OFD_CUDA(scratch_alloc((void **)&tmp, sizeof(float) * n, h->stream));
   h->be->from_padded(h->s, tmp, field, level, h->stream);
   OFD_CUDA(cudaGetLastError());
   OFD_CUDA(cudaMemcpyAsync(host, tmp, sizeof(float) * n, cudaMemcpyDefault, h->stream));

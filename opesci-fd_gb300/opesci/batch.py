@@ -95,6 +95,7 @@ def prepare(shot, tuned=True, built=None):
     cfg, media, src, wav, ks, kv = built if built is not None else shot.build()
     sim = runtime.Simulation(cfg)
     sim.set_coefficients(1, ks, kv)
+    sim.set_het_ghost_coefficients()
     sim.set_media(*media)
     sim.set_source(src, wav)
     if tuned:

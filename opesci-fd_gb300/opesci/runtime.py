@@ -84,6 +84,7 @@ def load_library():
         'ofd_footprint': [P(ofd_config), P(ctypes.c_size_t)],
         'ofd_set_media_const': [h, ctypes.c_float, ctypes.c_float, ctypes.c_float],
         'ofd_set_coefficients': [h, ctypes.c_int, fptr, ctypes.c_int, fptr, ctypes.c_int],
+        'ofd_set_ghost_coefficients': [h, ctypes.c_int, fptr, ctypes.c_int],
         'ofd_set_media': [h, fptr, fptr, fptr],
         'ofd_set_media_async': [h, fptr, fptr, fptr],
         'ofd_upload_field': [h, ctypes.c_int, ctypes.c_int, fptr],
@@ -266,6 +267,44 @@ class Simulation(object):
             raise OFDError('the update expressions of this model (%s) do not match the prebuilt '
                            'CUDA expressions; regenerate csrc/generated' % key)
         self.set_coefficients(1 if grid.read else 0, tabs['stress'][1], tabs['velocity'][1])
+        self.set_ghost_coefficients_from_grid(grid)
+
+    def set_ghost_coefficients(self, het, kg):
+        kg = np.ascontiguousarray(kg, dtype=np.float32)
+        _check(self.lib.ofd_set_ghost_coefficients(self.h, int(het), _fptr(kg), len(kg)),
+               'ofd_set_ghost_coefficients')
+
+    def set_het_ghost_coefficients(self):
+        """For a heterogeneous (read-mode) model of space order 4 with
+        Levander faces and isotropic spacing, the ghost literal table from
+        the stored monomials (cuda_gen.het_ghost_table) without the symbolic
+        frontend; other models keep the restated ghost formulas.  Returns
+        True when set."""
+        from .templates import cuda_gen
+        c = self.cfg
+        if (c.space_order != 4 or c.storage == STORAGE['f64']
+                or any(c.free_surface[i] != BC['levander'] for i in range(6))
+                or not (c.spacing[0] == c.spacing[1] == c.spacing[2])):
+            return False
+        self.set_ghost_coefficients(1, cuda_gen.het_ghost_table(c.dt, c.spacing[0]))
+        return True
+
+    def set_ghost_coefficients_from_grid(self, grid):
+        """Space order 4 with Levander faces: evaluate the ghosts from the
+        grid's own printed ghost equations when their structure is the
+        prebuilt one (FP32/FP16/BF16 storage).  Returns True when set."""
+        from .templates import cuda_gen
+        if self.cfg.storage == STORAGE['f64']:
+            return False
+        tab = cuda_gen.ghost_table(grid)
+        if tab is None:
+            return False
+        key = 'so4_%s' % ('het' if grid.read else 'const')
+        pre = cuda_gen.prebuilt_signatures().get(key, {})
+        if pre.get('ghost') != tab[0]:
+            return False
+        self.set_ghost_coefficients(1 if grid.read else 0, tab[1])
+        return True
 
     def set_media_const(self, beta, lam, mu):
         _check(self.lib.ofd_set_media_const(self.h, beta, lam, mu), 'ofd_set_media_const')

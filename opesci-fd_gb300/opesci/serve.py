@@ -113,6 +113,7 @@ def open_request(req, built, tuned=True):
                             storage=req.storage, free_surface=list(cfg.free_surface), field_scale=scales)
     sim = runtime.Simulation(c)
     sim.set_coefficients(1, ks, kv)
+    sim.set_het_ghost_coefficients()
     sim.set_media(*media)
     sim.set_source(src, wav)
     if tuned and req.storage == 'f32':

@@ -17,11 +17,13 @@ spacing or media values; each model's structure is checked against the
 signature of the generated header before its table is used.
 
 ``python -m opesci.templates.cuda_gen`` (from opesci-fd_gb300/) regenerates
-csrc/generated/sweeps_gen.cuh and signatures.json for space orders 2-8 with
-constant and heterogeneous media.
+csrc/generated/sweeps_gen.cuh, ghosts_gen.cuh (the space-order-4 Levander
+ghost expressions) and signatures.json for space orders 2-8 with constant and
+heterogeneous media.
 """
 import hashlib
 import json
+import math
 import os
 import re
 from fractions import Fraction
@@ -183,6 +185,8 @@ def generate_headers(outdir):
     lines.append('}  // namespace ofd')
     with open(os.path.join(outdir, 'sweeps_gen.cuh'), 'w') as f:
         f.write('\n'.join(lines) + '\n')
+    generate_ghost_header(outdir, sigs)
+    sigs['so4_het']['unit_ghost'] = het_ghost_units()
     with open(os.path.join(outdir, 'signatures.json'), 'w') as f:
         json.dump(sigs, f, indent=1, sort_keys=True)
     return sigs
@@ -224,6 +228,216 @@ def prebuilt_signatures():
                         'csrc', 'generated', 'signatures.json')
     with open(path) as f:
         return json.load(f)
+
+
+
+
+# ----------------------------------------------------------------- ghosts
+#
+# The Levander free-surface ghosts of space order 4 (fields.py:192-381,
+# applied by staggeredgrid.py:754-864) are printed the same way: the
+# expanded, constant-folded ghost equations of the frontend (transform_bc,
+# media resolved in read mode) become device expressions with their literals
+# in a run-time table KG.  Array references are given as offsets from the
+# ghost row's point on the boundary plane b (b = m on the lower face,
+# dim - m - 1 on the upper), so the text does not depend on the grid size:
+#   F[_tL][i][j][k] -> A(F_F, L, ox, oy, oz),  med[i][j][k] -> A.m(M_med, ox, oy, oz).
+# pow(m, 2) of the reference's C (a double result, which makes the rest of
+# the sum double in C) becomes ofd_pow2(m), the exact double square.
+# Every expression is a case of a switch over (component, face normal, side).
+
+_GARR = re.compile(r'\b(U|V|W|Txx|Tyy|Tzz|Txy|Tyz|Txz)\[_t([01])\]\[([^\]]+)\]\[([^\]]+)\]\[([^\]]+)\]')
+_GMED = re.compile(r'\b(lambda|mu12|mu13|mu23|mu|beta1|beta2|beta3)\[([^\]]+)\]\[([^\]]+)\]\[([^\]]+)\]')
+_GPOW = re.compile(r'pow\((A\.m\([^()]*\)), 2\)')
+GHOST_STRESS = ['Txx', 'Tyy', 'Tzz']
+GHOST_VEL = ['U', 'V', 'W']
+
+
+def _ghost_offsets(idx, d, b):
+    """Offsets (ox, oy, oz) of three printed indices; axis d holds a plane
+    number (relative to b), the others loop variables with offsets."""
+    out = []
+    for axis, t in enumerate(idx):
+        t = t.strip()
+        if axis == d:
+            if not re.fullmatch(r'\d+', t):
+                raise ValueError('unexpected face-normal index %r' % t)
+            out.append(int(t) - b)
+            continue
+        m = re.fullmatch(r'([xyz])(?: ([+-]) (\d+))?', t)
+        if not m or 'xyz'.index(m.group(1)) != axis:
+            raise ValueError('unexpected in-plane index %r on axis %d' % (t, axis))
+        out.append(0 if m.group(2) is None else (int(m.group(3)) if m.group(2) == '+' else -int(m.group(3))))
+    return out
+
+
+def _ghost_rhs(grid, field, d, side):
+    """(lhs, rhs) C texts of the ghost equations of ``field`` on face
+    (d, side), media resolved in read mode."""
+    from ..codeprinter import ccode_eq
+    out = []
+    for bc in grid.transform_bc(field, d + 1, side):
+        if grid.read:
+            bc = grid.resolve_media_params(bc)
+        s = ccode_eq(bc).replace('[_t + 1]', '[_t1]').replace('[_t]', '[_t0]')
+        lhs, rhs = s.split(' = ', 1)
+        out.append((lhs, rhs))
+    return out
+
+
+def ghost_text(grid):
+    """(cases, literal strings): cases = [(kind, comp, d, side, device text)]
+    for the Levander ghosts of a space-order-4 grid with free surfaces on all
+    faces; kind 'stress' (normal-stress recompute) or 'velocity'."""
+    grid.create_const_dict()
+    m = grid.margin.value
+    dims = [dd.value for dd in grid.dim]
+    by = {f.label.name: f for f in grid.fields}
+    cases, lits = [], []
+
+    def device(rhs, d, b):
+        parts, pos = [], 0
+        for mm in _LIT.finditer(rhs):
+            parts.append(rhs[pos:mm.start()])
+            parts.append('K[%d]' % len(lits))
+            lits.append(mm.group(1))
+            pos = mm.end()
+        parts.append(rhs[pos:])
+        t = ''.join(parts)
+        t = _GARR.sub(lambda a: 'A(%s, %s, %s)' % (_FIELD[a.group(1)], a.group(2),
+                                                 ', '.join(str(v) for v in _ghost_offsets(a.group(3, 4, 5), d, b))), t)
+        t = _GMED.sub(lambda a: 'A.m(%s, %s)' % (_MEDIA[a.group(1)],
+                                               ', '.join(str(v) for v in _ghost_offsets(a.group(2, 3, 4), d, b))), t)
+        t = _GPOW.sub(lambda a: 'ofd_pow2(%s)' % a.group(1), t)
+        if '[' in t.replace('K[', '') or 'pow(' in t:
+            raise ValueError('unsupported reference in ghost expression: %s' % t[:200])
+        return t
+
+    for ci, name in enumerate(GHOST_STRESS):
+        for d in range(3):
+            if d == ci:
+                continue
+            for side in range(2):
+                eqs = _ghost_rhs(grid, by[name], d, side)
+                if len(eqs) != 1:
+                    raise ValueError('expected one recompute equation for %s on face %d/%d' % (name, d, side))
+                b = m if side == 0 else dims[d] - m - 1
+                cases.append(('stress', ci, d, side, device(eqs[0][1], d, b)))
+    for d in range(3):
+        for ci, name in enumerate(GHOST_VEL):
+            for side in range(2):
+                eqs = _ghost_rhs(grid, by[name], d, side)
+                if len(eqs) != 1:
+                    raise ValueError('expected one ghost equation for %s on face %d/%d' % (name, d, side))
+                b = m if side == 0 else dims[d] - m - 1
+                cases.append(('velocity', ci, d, side, device(eqs[0][1], d, b)))
+    return cases, lits
+
+
+def ghost_signature(cases):
+    canon = '\n'.join('%s %d %d %d %s' % (k, c, d, s, re.sub(r'K\[\d+\]', 'K', t)) for k, c, d, s, t in cases)
+    return hashlib.sha1(canon.encode()).hexdigest()[:16]
+
+
+def ghost_table(grid):
+    """(signature, float32 literal table) of a space-order-4 grid's
+    Levander ghost expressions, or None when the grid has other ghosts."""
+    if grid.order[1] != 4:
+        return None
+    fs = getattr(grid, 'free_surface', {})
+    if len(fs) != 6 or any(v != 'levander' for v in fs.values()):
+        return None
+    cases, lits = ghost_text(grid)
+    return ghost_signature(cases), np.array([decimal_to_f32(t) for t in lits], dtype=np.float32)
+
+
+def _ghost_variant_grid(hetero):
+    from ..models import elastic_grid
+    if hetero:
+        return elastic_grid((130.0, 130.0, 130.0), (13, 13, 13), 7e-4, 7e-3, space_order=4,
+                            read=True, rho_file='r', vp_file='p', vs_file='s', analytic=False,
+                            free_surface=True)
+    return elastic_grid((1.0, 1.0, 1.0), (13, 13, 13), 3e-3, 3e-2, space_order=4,
+                        analytic=False, free_surface=True)
+
+
+def generate_ghost_header(outdir, sigs):
+    """ghosts_gen.cuh: GenGhost4<HET>::stress / ::velocity, and the ghost
+    signatures into ``sigs`` (so4_het / so4_const: 'ghost', 'nk_ghost')."""
+    lines = ['// GENERATED by opesci/templates/cuda_gen.py from the Levander ghost equations',
+             '// of StaggeredGrid at space order 4 (expanded, constant-folded, media',
+             '// resolved); do not edit.  Each case evaluates the reference generator\'s C',
+             '// expression of one ghost value with its literals taken from the table K;',
+             '// A(F, level, ox, oy, oz) is the field at level t0 (0) or t1 (1) at an offset',
+             '// from the ghost row\'s point on the boundary plane, A.m(M, ox, oy, oz) a medium.',
+             '#pragma once', '#include "ofd_common.cuh"', '', 'namespace ofd {', '',
+             '// the exact double square of a float (pow(float, 2) of the reference\'s C++)',
+             '__device__ __forceinline__ double ofd_pow2(float v) { return (double)v * (double)v; }', '',
+             'template <int HET> struct GenGhost4 { static constexpr bool ok = false; };', '']
+    for het in (0, 1):
+        g = _ghost_variant_grid(het)
+        cases, lits = ghost_text(g)
+        key = 'so4_%s' % ('het' if het else 'const')
+        sigs.setdefault(key, {})['ghost'] = ghost_signature(cases)
+        sigs[key]['nk_ghost'] = len(lits)
+        lines.append('template <> struct GenGhost4<%d> {' % het)
+        lines.append('  static constexpr bool ok = true;')
+        lines.append('  static constexpr int NK = %d;' % len(lits))
+        for kind in ('stress', 'velocity'):
+            lines.append('  // %s ghost of component c on face normal d, side (0 lower, 1 upper)' %
+                         ('normal-stress recompute' if kind == 'stress' else 'velocity'))
+            lines.append('  template <class Acc, class KT>')
+            lines.append('  __device__ static float %s(int c, int d, int side, const Acc &A, const KT &K) {' % kind)
+            lines.append('    switch (c * 6 + d * 2 + side) {')
+            for k, c, d, side, t in cases:
+                if k == kind:
+                    lines.append('      case %d: return (float)(%s);' % (c * 6 + d * 2 + side, t))
+            lines.append('    }')
+            lines.append('    return 0.f;')
+            lines.append('  }')
+        lines.append('};')
+        lines.append('')
+    lines.append('}  // namespace ofd')
+    with open(os.path.join(outdir, 'ghosts_gen.cuh'), 'w') as f:
+        f.write('\n'.join(lines) + '\n')
+
+
+def _het_ghost_grid(dt, h):
+    from ..models import elastic_grid
+    return elastic_grid((h * 13, h * 13, h * 13), (13, 13, 13), dt, dt * 10, space_order=4, read=True,
+                        rho_file='r', vp_file='p', vs_file='s', analytic=False, free_surface=True)
+
+
+def het_ghost_units():
+    """Each literal of the heterogeneous space-order-4 ghost expressions is a
+    monomial r dt^a h^b (isotropic spacing h): [str(r), a, b] per literal,
+    from the tables at (dt, h) = (1, 1), (2, 1) and (1, 2); checked against
+    a table at (7e-4, 10)."""
+    _, l1 = ghost_text(_het_ghost_grid(1.0, 1.0))
+    _, l2 = ghost_text(_het_ghost_grid(2.0, 1.0))
+    _, l3 = ghost_text(_het_ghost_grid(1.0, 2.0))
+    _, l4 = ghost_text(_het_ghost_grid(7e-4, 10.0))
+    out = []
+    for a, b, c, d in zip(l1, l2, l3, l4):
+        ra, rb, rc = Fraction(a), Fraction(b), Fraction(c)
+        ea = math.log2(float(rb / ra))
+        eh = math.log2(float(rc / ra))
+        if abs(ea - round(ea)) > 1e-9 or abs(eh - round(eh)) > 1e-9:
+            raise RuntimeError('ghost literal is not a monomial in dt and h')
+        pred = float(ra) * 7e-4 ** round(ea) * 10.0 ** round(eh)
+        if abs(pred / float(Fraction(d)) - 1) > 1e-13:
+            raise RuntimeError('ghost literal check failed')
+        out.append([a, int(round(ea)), int(round(eh))])
+    return out
+
+
+def het_ghost_table(dt, h):
+    """Literal table of the heterogeneous space-order-4 Levander ghost
+    expressions for isotropic spacing h and time step dt, from the stored
+    monomials (the same values the frontend prints for that grid)."""
+    units = prebuilt_signatures()['so4_het']['unit_ghost']
+    return np.array([np.float32(float(Fraction(r)) * float(dt) ** a * float(h) ** b) for r, a, b in units],
+                    dtype=np.float32)
 
 
 if __name__ == '__main__':

@@ -77,6 +77,7 @@ def test_group_of_16bit_members_and_member_streams():
                                 free_surface=list(cfg.free_surface), field_scale=scales)
         sim = runtime.Simulation(c)
         sim.set_coefficients(1, ks, kv)
+        sim.set_het_ghost_coefficients()
         sim.set_media(*media)
         sim.set_source(src, wav)
         return sim

@@ -92,12 +92,12 @@ def test_heterogeneous_source_matches_oracle(tmp_path, so):
     errs = rel_errors(got, ref['fields'])
     assert max(errs.values()) < TOL, errs
     assert np.abs(got['Txx']).max() > 0
-    if so != 4:
-        # Robertsson ghosts are exact zeros and mirrors exact negations, and
-        # the sweeps evaluate the reference's own expression without
-        # contraction: the run is bit-identical to the reference's C++
-        for f in runtime.FIELDS:
-            assert np.array_equal(got[f], ref['fields'][f]), f
+    # the sweeps evaluate the reference's own printed expression without
+    # contraction; Robertsson ghosts (SO2/6/8) are exact zeros and mirrors, and
+    # the SO4 Levander ghosts are the printed ghost equations (generated
+    # ghost expressions): the run is bit-identical to the reference's C++
+    for f in runtime.FIELDS:
+        assert np.array_equal(got[f], ref['fields'][f]), f
 
 
 def test_legacy_gpu_reproduces_reference_test3d(tmp_path):
@@ -155,6 +155,7 @@ def run_random_state(so, n, faces, storage, mode, steps=6):
                             rounding=rounding)
     sim = runtime.Simulation(c)
     sim.set_coefficients(1, ks, kv)
+    sim.set_het_ghost_coefficients()
     sim.set_media(*media)
     sim.set_source(src, wav)
     rng = np.random.default_rng(so * 1000 + n)
