@@ -167,8 +167,14 @@ __device__ __forceinline__ void stress_bc_point(const BcArgs<S> &a, int d, int i
   if constexpr (R == 2 && sizeof(S) <= 4) {
     if (a.gen) {
       const long o = base + b * sd;
-      const auto A = ghost_acc<S, COH>(a, o);
-      const float v = a.het ? GenGhost4<1>::stress(fi, d, side, A, a.kg) : GenGhost4<0>::stress(fi, d, side, A, a.kg);
+      float v;
+      if (a.rc) {
+        const int q = fi > d ? fi - 1 : fi;
+        v = a.rc[((d * 2 + side) * 2 + q) * a.rcs + (long)i1 * n2 + i2];
+      } else {
+        const auto A = ghost_acc<S, COH>(a, o);
+        v = a.het ? GenGhost4<1>::stress(fi, d, side, A, a.kg) : GenGhost4<0>::stress(fi, d, side, A, a.kg);
+      }
       T[o] = Storage<S>::store(v, a.sc[F]);
       return;
     }
@@ -189,6 +195,39 @@ __device__ __forceinline__ void stress_bc_point(const BcArgs<S> &a, int d, int i
                 a.c4[1] * (LV(ve, F_U + e, se) - LV(ve, F_U + e, -2 * se))) / a.h[e];
   const C t0 = Storage<S>::load(ldg<COH>(&a.f0[F][o]), a.inv[F]);
   T[o] = Storage<S>::store(t0 + a.dt * (K1 * Da + K2 * De), a.sc[F]);
+}
+
+// The generated normal-stress recompute values of one step, all face normals
+// at once, into rc (layout of BcArgs::rc): blockIdx.z = (d * 2 + side) * 2 + q.
+// Its inputs are the level-t0 stresses and velocities and the media, all
+// final before the step starts, so the runtime runs it on a second stream
+// while the stress sweep runs; the FP64 terms of the heterogeneous
+// expressions (pow(mu, 2) makes the rest of each sum double) then use the
+// FP64 units the memory-bound sweep leaves idle.  128-thread blocks with few
+// registers fit beside two sweep CTAs on an SM.
+template <int R, typename S>
+__global__ void __launch_bounds__(128) stress_recompute_kernel(BcArgs<S> a, float *rc) {
+  if constexpr (R == 2 && sizeof(S) <= 4) {
+    const Geom &g = a.g;
+    const int z = blockIdx.z, q = z & 1, side = (z >> 1) & 1, d = z >> 2;
+    int a1, a2;
+    plane_axes(d, a1, a2);
+    const int n1 = gdim(g, a1), n2 = gdim(g, a2), nd = gdim(g, d);
+    const int i2 = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i1 = blockIdx.y * blockDim.y + threadIdx.y;
+    const int m = g.m;
+    if (i1 < m + 1 || i1 >= n1 - m - 1 || i2 < m + 1 || i2 >= n2 - m - 1) return;
+    if (a.face[2 * d + side] != 1) return;
+    const int fi = q < d ? q : q + 1;
+    const int b = side == 0 ? m : nd - m - 1;
+    int c[3];
+    c[a1] = i1;
+    c[a2] = i2;
+    c[d] = b;
+    const auto A = ghost_acc<S, false>(a, lin(g, c[0], c[1], c[2]));
+    const float v = a.het ? GenGhost4<1>::stress(fi, d, side, A, a.kg) : GenGhost4<0>::stress(fi, d, side, A, a.kg);
+    rc[(long)z * a.rcs + (long)i1 * n2 + i2] = v;
+  }
 }
 
 // Stress ghosts of face normal a.d: blockIdx.z = field(0..5)*2 + side.
@@ -413,6 +452,99 @@ __global__ void __launch_bounds__(256) velocity_bc_merged_kernel(BcArgs<S> a, S 
       tzz[src_off] = Storage<S>::store(Storage<S>::load(tzz[src_off], 1.f / s2) - v, s2);
     }
     *step = st + 1;
+  }
+}
+
+// Velocity ghosts of face normal a.d with the generated ghost expressions
+// (space order 4, BcArgs::gen): as velocity_bc_merged_kernel, but each block
+// first computes the along-d component's ghost of its 32 x 8 in-plane points
+// and of the row and column beyond them into shared memory, once, and the
+// tangential ghosts read the fresh values from there (the merged kernel
+// evaluates each along-d ghost three times).  Robertsson faces as there.
+template <int R, typename S>
+__global__ void __launch_bounds__(256) velocity_bc_gen_kernel(BcArgs<S> a, S *txx, S *tyy, S *tzz, long src_off,
+                                                              const float *w, int nt, long *step, float s0, float s1,
+                                                              float s2) {
+  if constexpr (R == 2 && sizeof(S) <= 4) {
+    __shared__ float tile[9][33];
+    const Geom &g = a.g;
+    const int d = a.d;
+    int a1, a2;
+    plane_axes(d, a1, a2);
+    const int n1 = gdim(g, a1), n2 = gdim(g, a2), nd = gdim(g, d);
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int i2 = blockIdx.x * 32 + tx, i1 = blockIdx.y * 8 + ty;
+    auto inrange = [&](int p1, int p2) { return p1 >= 1 && p1 < n1 - 1 && p2 >= 1 && p2 < n2 - 1; };
+    const bool act = inrange(i1, i2);
+    const long sd = gstride(g, d);
+    const int Fd = F_U + d;
+    for (int side = 0; side < 2; ++side) {
+      const int fb = a.face[2 * d + side];   // the same for the whole block
+      if (fb == 0) continue;
+      if (fb == 2) {
+        if (act) {
+          velocity_bc_point<R, S, false>(a, d, 0, i1, i2, side);
+          velocity_bc_point<R, S, false>(a, d, 1, i1, i2, side);
+          velocity_bc_point<R, S, false>(a, d, 1, i1, i2, 2 + side);
+        }
+        continue;
+      }
+      const int b = side == 0 ? g.m : nd - g.m - 1;
+      auto ob_of = [&](int p1, int p2) {
+        int c[3];
+        c[a1] = p1;
+        c[a2] = p2;
+        c[d] = b;
+        return lin(g, c[0], c[1], c[2]);
+      };
+      auto fresh = [&](int p1, int p2) {
+        const float v = gen_velocity_ghost(a, d, d, side, ghost_acc<S, false>(a, ob_of(p1, p2)));
+        return (float)Storage<S>::load(Storage<S>::store(v, a.sc[Fd]), a.inv[Fd]);
+      };
+      const long ob = ob_of(i1, i2);
+      const long gpos = side == 0 ? ob - sd : ob;
+      float vg0 = 0.f;
+      if (act) {
+        const float vg = gen_velocity_ghost(a, d, d, side, ghost_acc<S, false>(a, ob));
+        a.f1[Fd][gpos] = Storage<S>::store(vg, a.sc[Fd]);
+        vg0 = (float)Storage<S>::load(Storage<S>::store(vg, a.sc[Fd]), a.inv[Fd]);
+      }
+      tile[ty][tx] = vg0;
+      if (ty == 7) tile[8][tx] = inrange(i1 + 1, i2) ? fresh(i1 + 1, i2) : 0.f;
+      if (tx == 31) tile[ty][32] = inrange(i1, i2 + 1) ? fresh(i1, i2 + 1) : 0.f;
+      __syncthreads();
+      if (act) {
+        for (int t = 0; t < 2; ++t) {
+          const int j = t == 0 ? a1 : a2;
+          const long sj = gstride(g, j);
+          // along-d ghost at the next point along j: the fresh value where the
+          // reference's face order has written it first, else the stored one
+          const bool in = t == 0 ? inrange(i1 + 1, i2) : inrange(i1, i2 + 1);
+          const float vgn = in ? (t == 0 ? tile[ty + 1][tx] : tile[ty][tx + 1])
+                               : (float)Storage<S>::load(a.f1[Fd][gpos + sj], a.inv[Fd]);
+          GhostAcc<S, false> A = ghost_acc<S, false>(a, ob);
+          A.fd = Fd;
+          A.go[d] = side == 0 ? -1 : 0;
+          A.ja = j;
+          A.v0 = vg0;
+          A.vn = vgn;
+          const int F = F_U + j;
+          const float val = gen_velocity_ghost(a, j, d, side, A);
+          a.f1[F][side == 0 ? ob - sd : ob + sd] = Storage<S>::store(val, a.sc[F]);
+        }
+      }
+      __syncthreads();
+    }
+    if (step != nullptr && d == 0 && i1 == 0 && i2 == 0) {
+      const long st = *step;
+      if (src_off >= 0 && st < nt) {
+        const float v = w[st] / 3;
+        txx[src_off] = Storage<S>::store(Storage<S>::load(txx[src_off], 1.f / s0) - v, s0);
+        tyy[src_off] = Storage<S>::store(Storage<S>::load(tyy[src_off], 1.f / s1) - v, s1);
+        tzz[src_off] = Storage<S>::store(Storage<S>::load(tzz[src_off], 1.f / s2) - v, s2);
+      }
+      *step = st + 1;
+    }
   }
 }
 

@@ -158,6 +158,12 @@ template <typename S> struct BcArgs {
   // formulas
   int gen, het;
   const float *kg;
+  // normal-stress recompute values precomputed for this step (stress ghosts
+  // with gen): rc[((d * 2 + side) * 2 + q) * rcs + i1 * n2(d) + i2], q the
+  // index of the recomputed normal stress among the two of face normal d;
+  // nullptr: evaluate in place
+  const float *rc;
+  long rcs;
 };
 
 }  // namespace ofd

@@ -47,6 +47,12 @@ struct DevState {
   int sr;              // 16-bit storage: stochastic rounding of the sweeps' stores
   int gen_ghost;       // space order 4: generated Levander ghost expressions (literals d_kg)
   float *d_kg;
+  // precomputed normal-stress recompute values (generated ghosts): 12 planes
+  // of rcs floats, computed on stream st2 beside the stress sweep
+  float *d_rc;
+  long rcs;
+  cudaStream_t st2;
+  cudaEvent_t ev_fork, ev_join;
   int nks, nkv;        // literal-table sizes (0 until ofd_set_coefficients)
   float Ks[OFD_MAX_K], Kv[OFD_MAX_K];
 };
@@ -263,6 +269,8 @@ struct Impl : Backend {
     a.gen = (R == 2 && sizeof(S) <= 4 && s.gen_ghost && s.d_kg) ? 1 : 0;
     a.het = s.het;
     a.kg = s.d_kg;
+    a.rc = nullptr;
+    a.rcs = s.rcs;
     return a;
   }
 
@@ -274,8 +282,26 @@ struct Impl : Backend {
     return dim3((n2 + 31) / 32, (n1 + 7) / 8, z);
   }
 
-  void stress_bc(const DevState &s, int t1, int t0, int recompute, cudaStream_t st) {
+  // the step's generated recompute values on the second stream, ordered after
+  // the work already queued on st; stress_bc waits for them (pre_join)
+  bool pre_recompute(const DevState &s, int t1, int t0, cudaStream_t st) {
+    if (!(R == 2 && sizeof(S) <= 4 && s.gen_ghost && s.d_kg && s.d_rc && s.st2 && !s.legacy)) return false;
+    BcArgs<S> a = bc_args(s, t1, t0, 1);
+    cudaEventRecord(s.ev_fork, st);
+    cudaStreamWaitEvent(s.st2, s.ev_fork, 0);
+    const Geom &g = s.g;
+    const int nmax = std::max(g.n1, std::max(g.n2, g.n3));
+    stress_recompute_kernel<R, S><<<dim3((nmax + 31) / 32, (nmax + 3) / 4, 12), dim3(32, 4), 0, s.st2>>>(a, s.d_rc);
+    cudaEventRecord(s.ev_join, s.st2);
+    return true;
+  }
+
+  void stress_bc(const DevState &s, int t1, int t0, int recompute, cudaStream_t st, bool pre = false) {
     BcArgs<S> a = bc_args(s, t1, t0, recompute);
+    if (pre) {
+      cudaStreamWaitEvent(st, s.ev_join, 0);
+      a.rc = s.d_rc;
+    }
     for (int d = 0; d < 3; ++d) {
       a.d = d;
       stress_bc_kernel<R, S><<<face_grid(s.g, d, 12), dim3(32, 8), 0, st>>>(a);
@@ -289,9 +315,14 @@ struct Impl : Backend {
     BcArgs<S> a = bc_args(s, t1, t1, 0);
     for (int d = 0; d < 3; ++d) {
       a.d = d;
-      velocity_bc_merged_kernel<R, S><<<face_grid(s.g, d, 1), dim3(32, 8), 0, st>>>(
-          a, fp(s, F_TXX, t1), fp(s, F_TYY, t1), fp(s, F_TZZ, t1), with_source ? s.src_off : -1L, s.d_wav, s.nt,
-          with_source ? s.d_step : nullptr, s.scale[F_TXX], s.scale[F_TYY], s.scale[F_TZZ]);
+      if (a.gen)
+        velocity_bc_gen_kernel<R, S><<<face_grid(s.g, d, 1), dim3(32, 8), 0, st>>>(
+            a, fp(s, F_TXX, t1), fp(s, F_TYY, t1), fp(s, F_TZZ, t1), with_source ? s.src_off : -1L, s.d_wav, s.nt,
+            with_source ? s.d_step : nullptr, s.scale[F_TXX], s.scale[F_TYY], s.scale[F_TZZ]);
+      else
+        velocity_bc_merged_kernel<R, S><<<face_grid(s.g, d, 1), dim3(32, 8), 0, st>>>(
+            a, fp(s, F_TXX, t1), fp(s, F_TYY, t1), fp(s, F_TZZ, t1), with_source ? s.src_off : -1L, s.d_wav, s.nt,
+            with_source ? s.d_step : nullptr, s.scale[F_TXX], s.scale[F_TYY], s.scale[F_TZZ]);
     }
   }
 
@@ -356,10 +387,11 @@ struct Impl : Backend {
     const int t1 = 1 - t0;
     auto rec = [&](int i) { if (ev) cudaEventRecord(ev->ev[i], st); };
     rec(0);
+    const bool pre = pre_recompute(s, t1, t0, st);
     sweeps(s, t0, true, st);
     rec(1);
     rec(2);
-    stress_bc(s, t1, t0, s.legacy ? 0 : 1, st);
+    stress_bc(s, t1, t0, s.legacy ? 0 : 1, st, pre);
     rec(3);
     rec(4);
     sweeps(s, t0, false, st);
@@ -372,8 +404,10 @@ struct Impl : Backend {
 
   int launches_per_step(const DevState &s) const override {
     // 2 sweeps + 3 stress-ghost phases + 3 velocity-ghost phases (the first
-    // carries the source and the step counter) + receivers, if any
-    return 2 + 3 + 3 + (s.nrec > 0 ? 1 : 0);
+    // carries the source and the step counter) + receivers, if any + the
+    // precomputed normal-stress recompute of the generated ghosts, if any
+    const bool pre = R == 2 && sizeof(S) <= 4 && s.gen_ghost && s.d_kg && s.d_rc && s.st2 && !s.legacy;
+    return 2 + 3 + 3 + (s.nrec > 0 ? 1 : 0) + (pre ? 1 : 0);
   }
 
   void boundary_init(const DevState &s, int level, cudaStream_t st) override {

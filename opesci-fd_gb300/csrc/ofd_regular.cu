@@ -19,6 +19,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 
 #include <cuda_runtime.h>
 
@@ -267,6 +268,27 @@ int copy_level(ofd_regular *h, int level, const void *src, void *dst, cudaMemcpy
 
 }  // namespace
 
+// The ring sweep's dynamic shared memory limit (a per-function, per-device
+// attribute shared by every handle): raised to the largest ring a handle of
+// this process has needed so far on the current device, never lowered, so
+// handles of different margins coexist; the direct sweep uses none.
+static cudaError_t raise_ring_limit(size_t es, size_t bytes) {
+  static std::mutex mu;
+  static size_t set_f32[64] = {}, set_f64[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) dev = 63;
+  std::lock_guard<std::mutex> lock(mu);
+  size_t &cur = es == 4 ? set_f32[dev] : set_f64[dev];
+  if (bytes <= cur) return cudaSuccess;
+  e = es == 4 ? cudaFuncSetAttribute(regular_sweep_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes)
+              : cudaFuncSetAttribute(regular_sweep_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)bytes);
+  if (e == cudaSuccess) cur = bytes;
+  return e;
+}
+
 extern "C" {
 
 int ofd_regular_create(const ofd_regular_config *cfg, ofd_regular **out) {
@@ -312,16 +334,7 @@ int ofd_regular_create(const ofd_regular_config *cfg, ofd_regular **out) {
   if (e == cudaSuccess) e = cudaMalloc(&h->raw, (size_t)h->level * 3 * h->es);
   if (e == cudaSuccess) e = cudaMemsetAsync(h->raw, 0, (size_t)h->level * 3 * h->es, h->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-  if (e == cudaSuccess) {
-    // the largest ring any handle of this type may need, so that handles of
-    // different margins coexist; each launch asks for its own size
-    if (h->es == 4)
-      e = cudaFuncSetAttribute(regular_sweep_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)ring_bytes(MAX_MARGIN, 4));
-    else
-      e = cudaFuncSetAttribute(regular_sweep_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)ring_bytes(MAX_MARGIN, 8));
-  }
+  if (e == cudaSuccess && h->variant == 1) e = raise_ring_limit(h->es, h->smem);
   if (e != cudaSuccess) {
     const int code = e == cudaErrorMemoryAllocation ? OFD_ENOMEM : OFD_ECUDA;
     if (h->raw) cudaFree(h->raw);

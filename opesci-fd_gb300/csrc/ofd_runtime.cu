@@ -1,6 +1,7 @@
 // Device runtime of the opesci-fd elastic hot path: handle lifecycle, HBM
 // layout, media preprocessing, transfers and the time loop, exported through
 // the C ABI of include/ofd.h.
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <cstdarg>
@@ -327,6 +328,12 @@ int ofd_footprint(const ofd_config *cfg, size_t *bytes) {
   int mz0;
   Geom mg = media_geom(cfg, &mz0);
   *bytes = (size_t)L.field_elems * L.esize * NF + (size_t)mg.level * sizeof(float) * NM + 4096;
+  if (cfg->space_order == 4) {
+    // generated-ghost buffers: twelve recompute planes and the literal table
+    const long a = std::max((long)cfg->dim[1] * cfg->dim[2],
+                            std::max((long)cfg->dim[0] * cfg->dim[2], (long)cfg->dim[0] * cfg->dim[1]));
+    *bytes += sizeof(float) * 12 * (size_t)a + 8192;
+  }
   return OFD_OK;
 }
 
@@ -401,6 +408,10 @@ int ofd_create(const ofd_config *cfg, ofd_handle **out) {
   h->s.sr = cfg->rounding == OFD_ROUND_STOCHASTIC ? 1 : 0;
   h->s.gen_ghost = 0;
   h->s.d_kg = nullptr;
+  h->s.d_rc = nullptr;
+  h->s.rcs = 0;
+  h->s.st2 = nullptr;
+  h->s.ev_fork = h->s.ev_join = nullptr;
   h->s.dt = cfg->dt;
   for (int i = 0; i < 3; ++i) h->s.h[i] = cfg->spacing[i];
   for (int k = 0; k < 4; ++k) h->s.c[k] = cfg->weights[k];
@@ -447,6 +458,13 @@ int ofd_destroy(ofd_handle *h) {
   delete h->maps;
   if (h->s.d_wav) cudaFree(h->s.d_wav);
   if (h->s.d_kg) cudaFree(h->s.d_kg);
+  if (h->s.d_rc) cudaFree(h->s.d_rc);
+  if (h->s.st2) {
+    cudaStreamSynchronize(h->s.st2);
+    cudaStreamDestroy(h->s.st2);
+  }
+  if (h->s.ev_fork) cudaEventDestroy(h->s.ev_fork);
+  if (h->s.ev_join) cudaEventDestroy(h->s.ev_join);
   if (h->s.d_rec) cudaFree(h->s.d_rec);
   if (h->s.d_traces) cudaFree(h->s.d_traces);
   if (h->fields_raw) cudaFree(h->fields_raw);
@@ -499,6 +517,17 @@ int ofd_set_ghost_coefficients(ofd_handle *h, int het, const float *kg, int nkg)
       return fail(OFD_EINVAL, "generated ghost expressions need Levander free surfaces on all six faces");
   OFD_CUDA(cudaStreamSynchronize(h->stream));
   if (!h->s.d_kg) OFD_CUDA(cudaMalloc((void **)&h->s.d_kg, sizeof(float) * (size_t)want));
+  if (!h->s.d_rc) {
+    // recompute values of one step (12 face planes), computed on a second
+    // stream while the stress sweep runs
+    const Geom &g = h->s.g;
+    const long rcs = std::max((long)g.n2 * g.n3, std::max((long)g.n1 * g.n3, (long)g.n1 * g.n2));
+    OFD_CUDA(cudaMalloc((void **)&h->s.d_rc, sizeof(float) * 12 * (size_t)rcs));
+    h->s.rcs = rcs;
+    OFD_CUDA(cudaStreamCreateWithFlags(&h->s.st2, cudaStreamNonBlocking));
+    OFD_CUDA(cudaEventCreateWithFlags(&h->s.ev_fork, cudaEventDisableTiming));
+    OFD_CUDA(cudaEventCreateWithFlags(&h->s.ev_join, cudaEventDisableTiming));
+  }
   OFD_CUDA(cudaMemcpyAsync(h->s.d_kg, kg, sizeof(float) * (size_t)nkg, cudaMemcpyHostToDevice, h->stream));
   OFD_CUDA(cudaStreamSynchronize(h->stream));
   h->s.gen_ghost = 1;

@@ -219,6 +219,33 @@ def run_grouped(shots, budget_bytes=150e9, keep=None, built=None, chunk_planes=0
     return time.perf_counter() - t0, outs
 
 
+EDGE_CLASSES = ((32, 64), (64, 96), (96, 128), (128, 193))
+
+
+def breakdown(shots, built, budget_bytes=150e9):
+    """Where the batched speed-up comes from: the shots binned by grid edge
+    and space order, each bin run grouped and one by one on its own.
+    Returns per bin the shot count, its share of all grid-point updates and
+    both arms' time and GLUP/s; with the bins' shares the whole workload's
+    speed-up is bounded by sum(share) / sum(share / bin speed-up)."""
+    total = sum(s.lups for s in shots)
+    out = []
+    for so in sorted({s.so for s in shots}):
+        for lo, hi in EDGE_CLASSES:
+            idx = [i for i, s in enumerate(shots) if s.so == so and lo <= s.n < hi]
+            if not idx:
+                continue
+            sub = [shots[i] for i in idx]
+            sb = [built[i] for i in idx]
+            lups = sum(s.lups for s in sub)
+            tg, _ = run_grouped(sub, budget_bytes=budget_bytes, built=sb)
+            to, _ = run_one_by_one(sub, built=sb)
+            out.append({'space_order': so, 'edge': [lo, hi - 1], 'shots': len(sub), 'lup_share': lups / total,
+                        'grouped_s': tg, 'one_by_one_s': to, 'grouped_glups': lups / tg / 1e9,
+                        'one_by_one_glups': lups / to / 1e9, 'speedup': to / tg})
+    return out
+
+
 def _footprint(shot):
     m = shot.so // 2
     dims = (shot.n + 2 * m,) * 3
@@ -233,6 +260,8 @@ def main():
     ap.add_argument('--budget-gb', type=float, default=150.0)
     ap.add_argument('--skip-one-by-one', action='store_true')
     ap.add_argument('--chunk-planes', type=int, default=0, help='x planes per sweep CTA in groups (0: heuristic)')
+    ap.add_argument('--breakdown', action='store_true',
+                    help='also run every (space order, edge) bin grouped and one by one on its own')
     args = ap.parse_args()
     os.environ.setdefault('CUDA_DEVICE_MAX_CONNECTIONS', '32')
     # under torchrun: one replica per GPU, shots split round robin
@@ -261,6 +290,8 @@ def main():
         to, _ = run_one_by_one(shots, built=built)
         res.update({'one_by_one_s': to, 'one_by_one_glups': lups / to / 1e9, 'speedup': to / tg,
                     'speedup_streams': to / tb})
+    if args.breakdown:
+        res['breakdown'] = breakdown(shots, built, budget_bytes=args.budget_gb * 1e9)
     res.update({'rank': rank, 'world': world})
     print(json.dumps(res))
 
