@@ -455,25 +455,23 @@ __global__ void __launch_bounds__(256) velocity_bc_merged_kernel(BcArgs<S> a, S 
   }
 }
 
-// Velocity ghosts of face normal a.d with the generated ghost expressions
-// (space order 4, BcArgs::gen): as velocity_bc_merged_kernel, but each block
-// first computes the along-d component's ghost of its 32 x 8 in-plane points
-// and of the row and column beyond them into shared memory, once, and the
-// tangential ghosts read the fresh values from there (the merged kernel
+// Velocity ghosts of face normal d with the generated ghost expressions
+// (space order 4, BcArgs::gen) for one 32 x 8 block of in-plane points
+// (i1, i2) = (by * 8 + ty, bx * 32 + tx): as velocity_bc_merged_point, but
+// the block first computes the along-d component's ghost of its points and
+// of the row and column beyond them into shared memory, once, and the
+// tangential ghosts read the fresh values from there (the merged form
 // evaluates each along-d ghost three times).  Robertsson faces as there.
+// Every thread of the block calls it (it synchronises the block).
 template <int R, typename S>
-__global__ void __launch_bounds__(256) velocity_bc_gen_kernel(BcArgs<S> a, S *txx, S *tyy, S *tzz, long src_off,
-                                                              const float *w, int nt, long *step, float s0, float s1,
-                                                              float s2) {
+__device__ __forceinline__ void velocity_gen_block(const BcArgs<S> &a, int d, int i1, int i2) {
   if constexpr (R == 2 && sizeof(S) <= 4) {
     __shared__ float tile[9][33];
     const Geom &g = a.g;
-    const int d = a.d;
     int a1, a2;
     plane_axes(d, a1, a2);
     const int n1 = gdim(g, a1), n2 = gdim(g, a2), nd = gdim(g, d);
     const int tx = threadIdx.x, ty = threadIdx.y;
-    const int i2 = blockIdx.x * 32 + tx, i1 = blockIdx.y * 8 + ty;
     auto inrange = [&](int p1, int p2) { return p1 >= 1 && p1 < n1 - 1 && p2 >= 1 && p2 < n2 - 1; };
     const bool act = inrange(i1, i2);
     const long sd = gstride(g, d);
@@ -535,16 +533,27 @@ __global__ void __launch_bounds__(256) velocity_bc_gen_kernel(BcArgs<S> a, S *tx
       }
       __syncthreads();
     }
-    if (step != nullptr && d == 0 && i1 == 0 && i2 == 0) {
-      const long st = *step;
-      if (src_off >= 0 && st < nt) {
-        const float v = w[st] / 3;
-        txx[src_off] = Storage<S>::store(Storage<S>::load(txx[src_off], 1.f / s0) - v, s0);
-        tyy[src_off] = Storage<S>::store(Storage<S>::load(tyy[src_off], 1.f / s1) - v, s1);
-        tzz[src_off] = Storage<S>::store(Storage<S>::load(tzz[src_off], 1.f / s2) - v, s2);
-      }
-      *step = st + 1;
+  }
+}
+
+// One launch per face normal with the generated ghost expressions; the
+// first also applies the source and advances the step counter, as
+// velocity_bc_merged_kernel.
+template <int R, typename S>
+__global__ void __launch_bounds__(256) velocity_bc_gen_kernel(BcArgs<S> a, S *txx, S *tyy, S *tzz, long src_off,
+                                                              const float *w, int nt, long *step, float s0, float s1,
+                                                              float s2) {
+  const int i2 = blockIdx.x * 32 + threadIdx.x, i1 = blockIdx.y * 8 + threadIdx.y;
+  velocity_gen_block<R, S>(a, a.d, i1, i2);
+  if (step != nullptr && a.d == 0 && i1 == 0 && i2 == 0) {
+    const long st = *step;
+    if (src_off >= 0 && st < nt) {
+      const float v = w[st] / 3;
+      txx[src_off] = Storage<S>::store(Storage<S>::load(txx[src_off], 1.f / s0) - v, s0);
+      tyy[src_off] = Storage<S>::store(Storage<S>::load(tyy[src_off], 1.f / s1) - v, s1);
+      tzz[src_off] = Storage<S>::store(Storage<S>::load(tzz[src_off], 1.f / s2) - v, s2);
     }
+    *step = st + 1;
   }
 }
 
@@ -613,6 +622,7 @@ struct GroupBc {
   long *step;
   float s0, s1, s2;
   RecArgs<S> rec;      // receivers of the member (nrec = 0: none)
+  int rbegin, rbx, rby; // generated-recompute launch: first block, 32 x 4 block grid of a face
 };
 
 template <typename S>
@@ -649,7 +659,8 @@ __global__ void __launch_bounds__(256) velocity_bc_group_kernel(const GroupBc<S>
   const int local = (int)blockIdx.x - e.begin[d];
   const int i2 = (local % e.bx[d]) * 32 + threadIdx.x;
   const int i1 = (local / e.bx[d]) * 8 + threadIdx.y;
-  velocity_bc_merged_point<R, S, false>(e.a, d, i1, i2);
+  if (e.a.gen) velocity_gen_block<R, S>(e.a, d, i1, i2);   // uniform in the block
+  else velocity_bc_merged_point<R, S, false>(e.a, d, i1, i2);
   if (d == 0 && local == 0 && threadIdx.x == 0 && threadIdx.y == 0 && e.step != nullptr) {
     const long st = *e.step;
     if (e.src_off >= 0 && st < e.nt) {
@@ -660,6 +671,52 @@ __global__ void __launch_bounds__(256) velocity_bc_group_kernel(const GroupBc<S>
       e.tzz[o] = Storage<S>::store(Storage<S>::load(e.tzz[o], 1.f / e.s2) - v, e.s2);
     }
     *e.step = st + 1;
+  }
+}
+
+// Generated normal-stress recompute values of every member that has them
+// (BcArgs::rc set), as stress_recompute_kernel: member blocks from rbegin,
+// each member's grid of 32 x 4 blocks rbx x rby x 12.
+template <int R, typename S>
+__global__ void __launch_bounds__(128) stress_recompute_group_kernel(const GroupBc<S> *__restrict__ tab, int n) {
+  if constexpr (R == 2 && sizeof(S) <= 4) {
+    __shared__ int s_member;
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+      int lo = 0, hi = n - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (tab[mid].rbegin <= (int)blockIdx.x) lo = mid;
+        else hi = mid - 1;
+      }
+      s_member = lo;
+    }
+    __syncthreads();
+    const GroupBc<S> &e = tab[s_member];
+    const BcArgs<S> &a = e.a;
+    if (!a.rc) return;
+    const int local = (int)blockIdx.x - e.rbegin;
+    const int per = e.rbx * e.rby;
+    if (local >= per * 12) return;
+    const int z = local / per, r = local - z * per;
+    const Geom &g = a.g;
+    const int q = z & 1, side = (z >> 1) & 1, d = z >> 2;
+    int a1, a2;
+    plane_axes(d, a1, a2);
+    const int n1 = gdim(g, a1), n2 = gdim(g, a2), nd = gdim(g, d);
+    const int i2 = (r % e.rbx) * 32 + threadIdx.x;
+    const int i1 = (r / e.rbx) * 4 + threadIdx.y;
+    const int m = g.m;
+    if (i1 < m + 1 || i1 >= n1 - m - 1 || i2 < m + 1 || i2 >= n2 - m - 1) return;
+    if (a.face[2 * d + side] != 1) return;
+    const int fi = q < d ? q : q + 1;
+    const int b = side == 0 ? m : nd - m - 1;
+    int c[3];
+    c[a1] = i1;
+    c[a2] = i2;
+    c[d] = b;
+    const auto A = ghost_acc<S, false>(a, lin(g, c[0], c[1], c[2]));
+    const float v = a.het ? GenGhost4<1>::stress(fi, d, side, A, a.kg) : GenGhost4<0>::stress(fi, d, side, A, a.kg);
+    const_cast<float *>(a.rc)[(long)z * a.rcs + (long)i1 * n2 + i2] = v;
   }
 }
 

@@ -282,18 +282,23 @@ struct Impl : Backend {
     return dim3((n2 + 31) / 32, (n1 + 7) / 8, z);
   }
 
-  // the step's generated recompute values on the second stream, ordered after
-  // the work already queued on st; stress_bc waits for them (pre_join)
-  bool pre_recompute(const DevState &s, int t1, int t0, cudaStream_t st) {
-    if (!(R == 2 && sizeof(S) <= 4 && s.gen_ghost && s.d_kg && s.d_rc && s.st2 && !s.legacy)) return false;
+  // The step's generated recompute values on the second stream.  fork marks
+  // the point on st after which they may start (the work already queued, the
+  // previous step's ghosts included); the kernel is launched after the stress
+  // sweep's launch, so the sweep's CTAs take the SMs first and the recompute
+  // blocks run in the room the sweep leaves (its FP64 work beside the
+  // memory-bound sweep).  stress_bc waits for ev_join.
+  static bool pre_ok(const DevState &s) {
+    return R == 2 && sizeof(S) <= 4 && s.gen_ghost && s.d_kg && s.d_rc && s.st2 && !s.legacy;
+  }
+  void pre_fork(const DevState &s, cudaStream_t st) { cudaEventRecord(s.ev_fork, st); }
+  void pre_recompute(const DevState &s, int t1, int t0) {
     BcArgs<S> a = bc_args(s, t1, t0, 1);
-    cudaEventRecord(s.ev_fork, st);
     cudaStreamWaitEvent(s.st2, s.ev_fork, 0);
     const Geom &g = s.g;
     const int nmax = std::max(g.n1, std::max(g.n2, g.n3));
     stress_recompute_kernel<R, S><<<dim3((nmax + 31) / 32, (nmax + 3) / 4, 12), dim3(32, 4), 0, s.st2>>>(a, s.d_rc);
     cudaEventRecord(s.ev_join, s.st2);
-    return true;
   }
 
   void stress_bc(const DevState &s, int t1, int t0, int recompute, cudaStream_t st, bool pre = false) {
@@ -387,8 +392,10 @@ struct Impl : Backend {
     const int t1 = 1 - t0;
     auto rec = [&](int i) { if (ev) cudaEventRecord(ev->ev[i], st); };
     rec(0);
-    const bool pre = pre_recompute(s, t1, t0, st);
+    const bool pre = pre_ok(s);
+    if (pre) pre_fork(s, st);
     sweeps(s, t0, true, st);
+    if (pre) pre_recompute(s, t1, t0);
     rec(1);
     rec(2);
     stress_bc(s, t1, t0, s.legacy ? 0 : 1, st, pre);
@@ -406,8 +413,7 @@ struct Impl : Backend {
     // 2 sweeps + 3 stress-ghost phases + 3 velocity-ghost phases (the first
     // carries the source and the step counter) + receivers, if any + the
     // precomputed normal-stress recompute of the generated ghosts, if any
-    const bool pre = R == 2 && sizeof(S) <= 4 && s.gen_ghost && s.d_kg && s.d_rc && s.st2 && !s.legacy;
-    return 2 + 3 + 3 + (s.nrec > 0 ? 1 : 0) + (pre ? 1 : 0);
+    return 2 + 3 + 3 + (s.nrec > 0 ? 1 : 0) + (pre_ok(s) ? 1 : 0);
   }
 
   void boundary_init(const DevState &s, int level, cudaStream_t st) override {
@@ -480,6 +486,11 @@ struct Impl : Backend {
     int sbc_blocks[3] = {0, 0, 0}, vbc_blocks[3] = {0, 0, 0};
     bool kd[2] = {false, false};   // [stress]: literal tables follow KMap (register-held literals)
     bool receivers = false;        // some member records traces
+    // generated-ghost recompute of the members that have it, on a second
+    // stream beside the stress sweep (as a single handle's step does)
+    int rc_blocks = 0;
+    cudaStream_t st2 = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
     std::vector<void *> raw;   // allocations (tables start 128-byte aligned inside them)
     // stream-ordered copy of a host table to a new 128-byte aligned device table
     template <typename T>
@@ -494,6 +505,9 @@ struct Impl : Backend {
     }
     ~Plan() override {
       for (void *p : raw) cudaFreeAsync(p, st);
+      if (st2) cudaStreamDestroy(st2);
+      if (fork) cudaEventDestroy(fork);
+      if (join) cudaEventDestroy(join);
     }
   };
 
@@ -585,6 +599,7 @@ struct Impl : Backend {
       const int t1 = 1 - t0;
       std::vector<GroupBc<S>> stab(n), vtab(n);
       int sb[3] = {0, 0, 0}, vb[3] = {0, 0, 0};
+      int rb = 0;
       for (int i = 0; i < n; ++i) {
         const DevState &s = *m[i];
         stab[i].a = bc_args(s, t1, t0, s.legacy ? 0 : 1);
@@ -600,6 +615,14 @@ struct Impl : Backend {
         }
         stab[i].step = nullptr;
         stab[i].src_off = -1;
+        stab[i].a.rc = pre_ok(s) ? s.d_rc : nullptr;
+        {
+          const int nmax = std::max(s.g.n1, std::max(s.g.n2, s.g.n3));
+          stab[i].rbx = vtab[i].rbx = (nmax + 31) / 32;
+          stab[i].rby = vtab[i].rby = (nmax + 3) / 4;
+          stab[i].rbegin = vtab[i].rbegin = rb;
+          if (stab[i].a.rc) rb += stab[i].rbx * stab[i].rby * 12;
+        }
         vtab[i].txx = fp(s, F_TXX, t1);
         vtab[i].tyy = fp(s, F_TYY, t1);
         vtab[i].tzz = fp(s, F_TZZ, t1);
@@ -617,6 +640,12 @@ struct Impl : Backend {
       for (int d = 0; d < 3; ++d) {
         pl->sbc_blocks[d] = sb[d];
         pl->vbc_blocks[d] = vb[d];
+      }
+      pl->rc_blocks = rb;
+      if (rb > 0 && !pl->st2) {
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&pl->st2, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&pl->fork, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&pl->join, cudaEventDisableTiming);
       }
       e = pl->upload(&pl->sbc[t0], stab.data(), n);
       if (e == cudaSuccess) e = pl->upload(&pl->vbc[t0], vtab.data(), n);
@@ -651,7 +680,15 @@ struct Impl : Backend {
         else launch(sweep_tiled_group<R, S, 0, false, false>, GV::THREADS, GV::SMEM, k);
       }
     };
+    const bool pre = pl->rc_blocks > 0 && pl->st2;
+    if (pre) cudaEventRecord(pl->fork, st);
     sweep(true);
+    if (pre) {
+      cudaStreamWaitEvent(pl->st2, pl->fork, 0);
+      stress_recompute_group_kernel<R, S><<<pl->rc_blocks, dim3(32, 4), 0, pl->st2>>>(pl->sbc[t0], n);
+      cudaEventRecord(pl->join, pl->st2);
+      cudaStreamWaitEvent(st, pl->join, 0);
+    }
     for (int d = 0; d < 3; ++d)
       stress_bc_group_kernel<R, S><<<pl->sbc_blocks[d], dim3(32, 8), 0, st>>>(pl->sbc[t0], n, d);
     sweep(false);
