@@ -198,35 +198,42 @@ __device__ __forceinline__ void stress_bc_point(const BcArgs<S> &a, int d, int i
 }
 
 // The generated normal-stress recompute values of one step, all face normals
-// at once, into rc (layout of BcArgs::rc): blockIdx.z = (d * 2 + side) * 2 + q.
-// Its inputs are the level-t0 stresses and velocities and the media, all
-// final before the step starts, so the runtime runs it on a second stream
-// while the stress sweep runs; the FP64 terms of the heterogeneous
-// expressions (pow(mu, 2) makes the rest of each sum double) then use the
-// FP64 units the memory-bound sweep leaves idle.  128-thread blocks with few
-// registers fit beside two sweep CTAs on an SM.
+// at once, into rc (layout of BcArgs::rc).  Its inputs are the level-t0
+// stresses and velocities and the media, all final before the step starts,
+// so the runtime runs it on a second stream beside the stress sweep; the
+// FP64 terms of the heterogeneous expressions (pow(mu, 2) makes the rest of
+// each sum double) then use the FP64 units the memory-bound sweep leaves
+// idle.  The grid is small (one 128-thread block per SM, grid-stride over
+// the 12 face planes) and is launched before the sweep, so all of it is
+// resident at once beside two sweep CTAs per SM (their registers leave room
+// for one such block) instead of queueing behind the sweep's waves.
 template <int R, typename S>
-__global__ void __launch_bounds__(128) stress_recompute_kernel(BcArgs<S> a, float *rc) {
+__global__ void __launch_bounds__(128) stress_recompute_kernel(BcArgs<S> a, float *rc, int nmax) {
   if constexpr (R == 2 && sizeof(S) <= 4) {
     const Geom &g = a.g;
-    const int z = blockIdx.z, q = z & 1, side = (z >> 1) & 1, d = z >> 2;
-    int a1, a2;
-    plane_axes(d, a1, a2);
-    const int n1 = gdim(g, a1), n2 = gdim(g, a2), nd = gdim(g, d);
-    const int i2 = blockIdx.x * blockDim.x + threadIdx.x;
-    const int i1 = blockIdx.y * blockDim.y + threadIdx.y;
     const int m = g.m;
-    if (i1 < m + 1 || i1 >= n1 - m - 1 || i2 < m + 1 || i2 >= n2 - m - 1) return;
-    if (a.face[2 * d + side] != 1) return;
-    const int fi = q < d ? q : q + 1;
-    const int b = side == 0 ? m : nd - m - 1;
-    int c[3];
-    c[a1] = i1;
-    c[a2] = i2;
-    c[d] = b;
-    const auto A = ghost_acc<S, false>(a, lin(g, c[0], c[1], c[2]));
-    const float v = a.het ? GenGhost4<1>::stress(fi, d, side, A, a.kg) : GenGhost4<0>::stress(fi, d, side, A, a.kg);
-    rc[(long)z * a.rcs + (long)i1 * n2 + i2] = v;
+    const long per = (long)nmax * nmax;
+    for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < 12 * per; it += (long)gridDim.x * blockDim.x) {
+      const int z = (int)(it / per);
+      const long r = it - z * per;
+      const int i1 = (int)(r / nmax), i2 = (int)(r % nmax);
+      const int q = z & 1, side = (z >> 1) & 1, d = z >> 2;
+      int a1, a2;
+      plane_axes(d, a1, a2);
+      const int n1 = gdim(g, a1), n2 = gdim(g, a2), nd = gdim(g, d);
+      if (i1 < m + 1 || i1 >= n1 - m - 1 || i2 < m + 1 || i2 >= n2 - m - 1) continue;
+      if (a.face[2 * d + side] != 1) continue;
+      const int fi = q < d ? q : q + 1;
+      const int b = side == 0 ? m : nd - m - 1;
+      int c[3];
+      c[a1] = i1;
+      c[a2] = i2;
+      c[d] = b;
+      const auto A = ghost_acc<S, false>(a, lin(g, c[0], c[1], c[2]));
+      const float v =
+          a.het ? GenGhost4<1>::stress(fi, d, side, A, a.kg) : GenGhost4<0>::stress(fi, d, side, A, a.kg);
+      rc[(long)z * a.rcs + (long)i1 * n2 + i2] = v;
+    }
   }
 }
 
@@ -675,48 +682,47 @@ __global__ void __launch_bounds__(256) velocity_bc_group_kernel(const GroupBc<S>
 }
 
 // Generated normal-stress recompute values of every member that has them
-// (BcArgs::rc set), as stress_recompute_kernel: member blocks from rbegin,
-// each member's grid of 32 x 4 blocks rbx x rby x 12.
+// (BcArgs::rc set), as stress_recompute_kernel: grid-stride over virtual
+// 32 x 4 blocks (member ranges from rbegin, each member's grid rbx x rby x 12).
 template <int R, typename S>
-__global__ void __launch_bounds__(128) stress_recompute_group_kernel(const GroupBc<S> *__restrict__ tab, int n) {
+__global__ void __launch_bounds__(128) stress_recompute_group_kernel(const GroupBc<S> *__restrict__ tab, int n,
+                                                                     int total) {
   if constexpr (R == 2 && sizeof(S) <= 4) {
-    __shared__ int s_member;
-    if (threadIdx.x == 0 && threadIdx.y == 0) {
+    for (int vb = blockIdx.x; vb < total; vb += gridDim.x) {
       int lo = 0, hi = n - 1;
       while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
-        if (tab[mid].rbegin <= (int)blockIdx.x) lo = mid;
+        if (tab[mid].rbegin <= vb) lo = mid;
         else hi = mid - 1;
       }
-      s_member = lo;
+      const GroupBc<S> &e = tab[lo];
+      const BcArgs<S> &a = e.a;
+      if (!a.rc) continue;
+      const int local = vb - e.rbegin;
+      const int per = e.rbx * e.rby;
+      if (local >= per * 12) continue;
+      const int z = local / per, r = local - z * per;
+      const Geom &g = a.g;
+      const int q = z & 1, side = (z >> 1) & 1, d = z >> 2;
+      int a1, a2;
+      plane_axes(d, a1, a2);
+      const int n1 = gdim(g, a1), n2 = gdim(g, a2), nd = gdim(g, d);
+      const int i2 = (r % e.rbx) * 32 + threadIdx.x;
+      const int i1 = (r / e.rbx) * 4 + threadIdx.y;
+      const int m = g.m;
+      if (i1 < m + 1 || i1 >= n1 - m - 1 || i2 < m + 1 || i2 >= n2 - m - 1) continue;
+      if (a.face[2 * d + side] != 1) continue;
+      const int fi = q < d ? q : q + 1;
+      const int b = side == 0 ? m : nd - m - 1;
+      int c[3];
+      c[a1] = i1;
+      c[a2] = i2;
+      c[d] = b;
+      const auto A = ghost_acc<S, false>(a, lin(g, c[0], c[1], c[2]));
+      const float v =
+          a.het ? GenGhost4<1>::stress(fi, d, side, A, a.kg) : GenGhost4<0>::stress(fi, d, side, A, a.kg);
+      const_cast<float *>(a.rc)[(long)z * a.rcs + (long)i1 * n2 + i2] = v;
     }
-    __syncthreads();
-    const GroupBc<S> &e = tab[s_member];
-    const BcArgs<S> &a = e.a;
-    if (!a.rc) return;
-    const int local = (int)blockIdx.x - e.rbegin;
-    const int per = e.rbx * e.rby;
-    if (local >= per * 12) return;
-    const int z = local / per, r = local - z * per;
-    const Geom &g = a.g;
-    const int q = z & 1, side = (z >> 1) & 1, d = z >> 2;
-    int a1, a2;
-    plane_axes(d, a1, a2);
-    const int n1 = gdim(g, a1), n2 = gdim(g, a2), nd = gdim(g, d);
-    const int i2 = (r % e.rbx) * 32 + threadIdx.x;
-    const int i1 = (r / e.rbx) * 4 + threadIdx.y;
-    const int m = g.m;
-    if (i1 < m + 1 || i1 >= n1 - m - 1 || i2 < m + 1 || i2 >= n2 - m - 1) return;
-    if (a.face[2 * d + side] != 1) return;
-    const int fi = q < d ? q : q + 1;
-    const int b = side == 0 ? m : nd - m - 1;
-    int c[3];
-    c[a1] = i1;
-    c[a2] = i2;
-    c[d] = b;
-    const auto A = ghost_acc<S, false>(a, lin(g, c[0], c[1], c[2]));
-    const float v = a.het ? GenGhost4<1>::stress(fi, d, side, A, a.kg) : GenGhost4<0>::stress(fi, d, side, A, a.kg);
-    const_cast<float *>(a.rc)[(long)z * a.rcs + (long)i1 * n2 + i2] = v;
   }
 }
 

@@ -109,6 +109,19 @@ Backend *make_backend_f64(int R);
 Backend *make_backend_f16(int R);
 Backend *make_backend_bf16(int R);
 
+// SMs of the current device (cached per device)
+inline int sm_count() {
+  static int cache[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+  if (!cache[dev]) {
+    int n = 0;
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    cache[dev] = n > 0 ? n : 152;
+  }
+  return cache[dev];
+}
+
 // ---- generic kernels ------------------------------------------------------
 
 template <typename S>
@@ -282,11 +295,10 @@ struct Impl : Backend {
     return dim3((n2 + 31) / 32, (n1 + 7) / 8, z);
   }
 
-  // The step's generated recompute values on the second stream.  fork marks
-  // the point on st after which they may start (the work already queued, the
-  // previous step's ghosts included); the kernel is launched after the stress
-  // sweep's launch, so the sweep's CTAs take the SMs first and the recompute
-  // blocks run in the room the sweep leaves (its FP64 work beside the
+  // The step's generated recompute values on the second stream, after the
+  // work already queued on st (the previous step's ghosts included), launched
+  // before the stress sweep with one 128-thread block per SM so that all of
+  // it is resident beside the sweep's two CTAs (its FP64 work beside the
   // memory-bound sweep).  stress_bc waits for ev_join.
   static bool pre_ok(const DevState &s) {
     return R == 2 && sizeof(S) <= 4 && s.gen_ghost && s.d_kg && s.d_rc && s.st2 && !s.legacy;
@@ -297,7 +309,7 @@ struct Impl : Backend {
     cudaStreamWaitEvent(s.st2, s.ev_fork, 0);
     const Geom &g = s.g;
     const int nmax = std::max(g.n1, std::max(g.n2, g.n3));
-    stress_recompute_kernel<R, S><<<dim3((nmax + 31) / 32, (nmax + 3) / 4, 12), dim3(32, 4), 0, s.st2>>>(a, s.d_rc);
+    stress_recompute_kernel<R, S><<<sm_count(), 128, 0, s.st2>>>(a, s.d_rc, nmax);
     cudaEventRecord(s.ev_join, s.st2);
   }
 
@@ -393,9 +405,11 @@ struct Impl : Backend {
     auto rec = [&](int i) { if (ev) cudaEventRecord(ev->ev[i], st); };
     rec(0);
     const bool pre = pre_ok(s);
-    if (pre) pre_fork(s, st);
+    if (pre) {
+      pre_fork(s, st);
+      pre_recompute(s, t1, t0);
+    }
     sweeps(s, t0, true, st);
-    if (pre) pre_recompute(s, t1, t0);
     rec(1);
     rec(2);
     stress_bc(s, t1, t0, s.legacy ? 0 : 1, st, pre);
@@ -681,14 +695,15 @@ struct Impl : Backend {
       }
     };
     const bool pre = pl->rc_blocks > 0 && pl->st2;
-    if (pre) cudaEventRecord(pl->fork, st);
-    sweep(true);
     if (pre) {
+      cudaEventRecord(pl->fork, st);
       cudaStreamWaitEvent(pl->st2, pl->fork, 0);
-      stress_recompute_group_kernel<R, S><<<pl->rc_blocks, dim3(32, 4), 0, pl->st2>>>(pl->sbc[t0], n);
+      const int grid = std::min(pl->rc_blocks, sm_count());
+      stress_recompute_group_kernel<R, S><<<grid, dim3(32, 4), 0, pl->st2>>>(pl->sbc[t0], n, pl->rc_blocks);
       cudaEventRecord(pl->join, pl->st2);
-      cudaStreamWaitEvent(st, pl->join, 0);
     }
+    sweep(true);
+    if (pre) cudaStreamWaitEvent(st, pl->join, 0);
     for (int d = 0; d < 3; ++d)
       stress_bc_group_kernel<R, S><<<pl->sbc_blocks[d], dim3(32, 8), 0, st>>>(pl->sbc[t0], n, d);
     sweep(false);
