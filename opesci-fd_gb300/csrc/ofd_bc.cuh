@@ -65,6 +65,15 @@ __device__ __forceinline__ long lin(const Geom &g, int x, int y, int z) {
   return (long)x * g.plane + (long)y * g.P + z;
 }
 
+// offset of the point with in-plane coordinates (p1, p2) (axes of
+// plane_axes(d)) and coordinate pd along d; no runtime-indexed arrays, so
+// nothing lands in local memory
+__device__ __forceinline__ long plane_lin(const Geom &g, int d, int p1, int p2, int pd) {
+  if (d == 0) return lin(g, pd, p1, p2);
+  if (d == 1) return lin(g, p1, pd, p2);
+  return lin(g, p1, p2, pd);
+}
+
 __device__ __forceinline__ int gdim(const Geom &g, int a) { return a == 0 ? g.n1 : (a == 1 ? g.n2 : g.n3); }
 
 // stride of axis a in elements
@@ -88,14 +97,14 @@ struct GhostAcc {
   const BcArgs<S> &a;
   long o;
   int fd;          // field whose fresh ghost values are used (-1: none)
-  int go[3];       // offset of that ghost at this point
+  int gd, gv;      // that ghost sits at offset gv along axis gd from this point
   int ja;          // axis of the neighbour holding vn
   float v0, vn;
   __device__ __forceinline__ float operator()(int f, int lvl, int ox, int oy, int oz) const {
     if (f == fd) {
-      const int e[3] = {ox - go[0], oy - go[1], oz - go[2]};
-      if (e[0] == 0 && e[1] == 0 && e[2] == 0) return v0;
-      if (e[ja] == 1 && e[(ja + 1) % 3] == 0 && e[(ja + 2) % 3] == 0) return vn;
+      const int ex = ox - (gd == 0 ? gv : 0), ey = oy - (gd == 1 ? gv : 0), ez = oz - (gd == 2 ? gv : 0);
+      if (ex == 0 && ey == 0 && ez == 0) return v0;
+      if (ex == (ja == 0) && ey == (ja == 1) && ez == (ja == 2)) return vn;
     }
     const S *p = lvl ? (const S *)a.f1[f] : a.f0[f];
     return (float)Storage<S>::load(ldg<COH>(&p[o + ox * a.g.plane + oy * a.g.P + oz]), a.inv[f]);
@@ -107,7 +116,7 @@ struct GhostAcc {
 
 template <typename S, bool COH>
 __device__ __forceinline__ GhostAcc<S, COH> ghost_acc(const BcArgs<S> &a, long o) {
-  return GhostAcc<S, COH>{a, o, -1, {0, 0, 0}, 0, 0.f, 0.f};
+  return GhostAcc<S, COH>{a, o, -1, 0, 0, 0, 0.f, 0.f};
 }
 
 // generated velocity ghost of component c on face (d, side) at point o of
@@ -115,6 +124,14 @@ __device__ __forceinline__ GhostAcc<S, COH> ghost_acc(const BcArgs<S> &a, long o
 template <class Acc, class S>
 __device__ __forceinline__ float gen_velocity_ghost(const BcArgs<S> &a, int c, int d, int side, const Acc &A) {
   return a.het ? GenGhost4<1>::velocity(c, d, side, A, a.kg) : GenGhost4<0>::velocity(c, d, side, A, a.kg);
+}
+
+// generated normal-stress recompute value of stress fi on face (d, side)
+template <class Acc, class S>
+__device__ __forceinline__ float gen_stress_recompute(const BcArgs<S> &a, int fi, int d, int side, const Acc &A) {
+  if (a.het)
+    return a.gsd ? GenGhost4<1>::stress_sd(fi, d, side, A, a.kg) : GenGhost4<1>::stress(fi, d, side, A, a.kg);
+  return a.gsd ? GenGhost4<0>::stress_sd(fi, d, side, A, a.kg) : GenGhost4<0>::stress(fi, d, side, A, a.kg);
 }
 
 // Stress ghosts of face normal d at in-plane point (i1, i2) for stress
@@ -136,9 +153,7 @@ __device__ __forceinline__ void stress_bc_point(const BcArgs<S> &a, int d, int i
   const bool normal = fi < 3;
   const int m = g.m;
   const int b = side == 0 ? m : nd - m - 1;
-  int c[3];
-  c[a1] = i1; c[a2] = i2; c[d] = 0;
-  const long base = lin(g, c[0], c[1], c[2]);
+  const long base = plane_lin(g, d, i1, i2, 0);
   const long sd = gstride(g, d);
   S *T = a.f1[F];
   if (d == dA || d == dB) {
@@ -173,7 +188,7 @@ __device__ __forceinline__ void stress_bc_point(const BcArgs<S> &a, int d, int i
         v = a.rc[((d * 2 + side) * 2 + q) * a.rcs + (long)i1 * n2 + i2];
       } else {
         const auto A = ghost_acc<S, COH>(a, o);
-        v = a.het ? GenGhost4<1>::stress(fi, d, side, A, a.kg) : GenGhost4<0>::stress(fi, d, side, A, a.kg);
+        v = gen_stress_recompute(a, fi, d, side, A);
       }
       T[o] = Storage<S>::store(v, a.sc[F]);
       return;
@@ -200,23 +215,23 @@ __device__ __forceinline__ void stress_bc_point(const BcArgs<S> &a, int d, int i
 // The generated normal-stress recompute values of one step, all face normals
 // at once, into rc (layout of BcArgs::rc).  Its inputs are the level-t0
 // stresses and velocities and the media, all final before the step starts,
-// so the runtime runs it on a second stream beside the stress sweep; the
+// so the runtime may run it on a second stream beside the stress sweep; the
 // FP64 terms of the heterogeneous expressions (pow(mu, 2) makes the rest of
 // each sum double) then use the FP64 units the memory-bound sweep leaves
-// idle.  The grid is small (one 128-thread block per SM, grid-stride over
-// the 12 face planes) and is launched before the sweep, so all of it is
-// resident at once beside two sweep CTAs per SM (their registers leave room
-// for one such block) instead of queueing behind the sweep's waves.
+// idle.  Grid-stride over virtual 32 x 4 tiles of the 12 face planes (lane:
+// i2, warp: i1), so that a small grid of a few blocks per SM covers it.
 template <int R, typename S>
-__global__ void __launch_bounds__(128) stress_recompute_kernel(BcArgs<S> a, float *rc, int nmax) {
+__global__ void __launch_bounds__(128) stress_recompute_kernel(const __grid_constant__ BcArgs<S> a, float *rc, int nmax) {
   if constexpr (R == 2 && sizeof(S) <= 4) {
     const Geom &g = a.g;
     const int m = g.m;
-    const long per = (long)nmax * nmax;
-    for (long it = blockIdx.x * (long)blockDim.x + threadIdx.x; it < 12 * per; it += (long)gridDim.x * blockDim.x) {
-      const int z = (int)(it / per);
-      const long r = it - z * per;
-      const int i1 = (int)(r / nmax), i2 = (int)(r % nmax);
+    const int tx = (nmax + 31) >> 5, ty = (nmax + 3) >> 2;
+    const int per = tx * ty;
+    for (int vb = blockIdx.x; vb < 12 * per; vb += gridDim.x) {
+      const int z = vb / per;
+      const int r = vb - z * per;
+      const int i1 = (r / tx) * 4 + (int)(threadIdx.x >> 5);
+      const int i2 = (r % tx) * 32 + (int)(threadIdx.x & 31);
       const int q = z & 1, side = (z >> 1) & 1, d = z >> 2;
       int a1, a2;
       plane_axes(d, a1, a2);
@@ -225,13 +240,9 @@ __global__ void __launch_bounds__(128) stress_recompute_kernel(BcArgs<S> a, floa
       if (a.face[2 * d + side] != 1) continue;
       const int fi = q < d ? q : q + 1;
       const int b = side == 0 ? m : nd - m - 1;
-      int c[3];
-      c[a1] = i1;
-      c[a2] = i2;
-      c[d] = b;
-      const auto A = ghost_acc<S, false>(a, lin(g, c[0], c[1], c[2]));
+      const auto A = ghost_acc<S, false>(a, plane_lin(g, d, i1, i2, b));
       const float v =
-          a.het ? GenGhost4<1>::stress(fi, d, side, A, a.kg) : GenGhost4<0>::stress(fi, d, side, A, a.kg);
+          gen_stress_recompute(a, fi, d, side, A);
       rc[(long)z * a.rcs + (long)i1 * n2 + i2] = v;
     }
   }
@@ -239,7 +250,7 @@ __global__ void __launch_bounds__(128) stress_recompute_kernel(BcArgs<S> a, floa
 
 // Stress ghosts of face normal a.d: blockIdx.z = field(0..5)*2 + side.
 template <int R, typename S>
-__global__ void __launch_bounds__(256) stress_bc_kernel(BcArgs<S> a) {
+__global__ void __launch_bounds__(256) stress_bc_kernel(const __grid_constant__ BcArgs<S> a) {
   const int i2 = blockIdx.x * blockDim.x + threadIdx.x;
   const int i1 = blockIdx.y * blockDim.y + threadIdx.y;
   stress_bc_point<R, S, false>(a, a.d, i1, i2, blockIdx.z >> 1, blockIdx.z & 1);
@@ -260,9 +271,7 @@ __device__ __forceinline__ void velocity_bc_point(const BcArgs<S> &a, int d, int
   if (fb == 0) return;
   const int m = g.m;
   const int b = side == 0 ? m : nd - m - 1;
-  int c[3];
-  c[a1] = i1; c[a2] = i2; c[d] = 0;
-  const long base = lin(g, c[0], c[1], c[2]);
+  const long base = plane_lin(g, d, i1, i2, 0);
   const long sd = gstride(g, d);
   const int comp = (sub == 0) ? d : ((zi >> 1) == 0 ? a1 : a2);
   const int F = F_U + comp;
@@ -326,10 +335,8 @@ __device__ __forceinline__ typename Storage<S>::C levander_normal_ghost(const Bc
   plane_axes(d, a1, a2);
   const int nd = gdim(g, d);
   const int b = side == 0 ? g.m : nd - g.m - 1;
-  int c[3];
-  c[a1] = i1; c[a2] = i2; c[d] = 0;
   const long sd = gstride(g, d);
-  const long ob = lin(g, c[0], c[1], c[2]) + b * sd;
+  const long ob = plane_lin(g, d, i1, i2, 0) + b * sd;
   const int F = F_U + d;
   auto LD = [&](int f, long off) -> C { return Storage<S>::load(ldg<COH>(&a.f1[f][off]), a.inv[f]); };
   const C lam = (C)a.media[M_LAM][ob], mu = (C)a.media[M_MU][ob];
@@ -370,9 +377,7 @@ __device__ __forceinline__ void velocity_bc_merged_point(const BcArgs<S> &a, int
       continue;
     }
     const int b = side == 0 ? g.m : nd - g.m - 1;
-    int c[3];
-    c[a1] = i1; c[a2] = i2; c[d] = 0;
-    const long base = lin(g, c[0], c[1], c[2]);
+    const long base = plane_lin(g, d, i1, i2, 0);
     const long ob = base + b * sd, obm = ob - sd;
     const long gpos = side == 0 ? obm : ob;        // where the along-d ghost lives
     if constexpr (R == 2 && sizeof(S) <= 4) {
@@ -394,7 +399,8 @@ __device__ __forceinline__ void velocity_bc_merged_point(const BcArgs<S> &a, int
                  : (float)Storage<S>::load(ldg<COH>(&a.f1[Fd][gpos + sj]), a.inv[Fd]);
           GhostAcc<S, COH> A = ghost_acc<S, COH>(a, ob);
           A.fd = Fd;
-          A.go[d] = side == 0 ? -1 : 0;
+          A.gd = d;
+          A.gv = side == 0 ? -1 : 0;
           A.ja = j;
           A.v0 = vg0;
           A.vn = vgn;
@@ -444,7 +450,7 @@ __device__ __forceinline__ void velocity_bc_merged_point(const BcArgs<S> &a, int
 // captured step graph replays with unchanged arguments: the wavelet sample is
 // picked on the device from the step counter.
 template <int R, typename S>
-__global__ void __launch_bounds__(256) velocity_bc_merged_kernel(BcArgs<S> a, S *txx, S *tyy, S *tzz, long src_off,
+__global__ void __launch_bounds__(256) velocity_bc_merged_kernel(const __grid_constant__ BcArgs<S> a, S *txx, S *tyy, S *tzz, long src_off,
                                                                  const float *w, int nt, long *step, float s0,
                                                                  float s1, float s2) {
   const int i2 = blockIdx.x * blockDim.x + threadIdx.x;
@@ -496,11 +502,7 @@ __device__ __forceinline__ void velocity_gen_block(const BcArgs<S> &a, int d, in
       }
       const int b = side == 0 ? g.m : nd - g.m - 1;
       auto ob_of = [&](int p1, int p2) {
-        int c[3];
-        c[a1] = p1;
-        c[a2] = p2;
-        c[d] = b;
-        return lin(g, c[0], c[1], c[2]);
+        return plane_lin(g, d, p1, p2, b);
       };
       auto fresh = [&](int p1, int p2) {
         const float v = gen_velocity_ghost(a, d, d, side, ghost_acc<S, false>(a, ob_of(p1, p2)));
@@ -529,7 +531,8 @@ __device__ __forceinline__ void velocity_gen_block(const BcArgs<S> &a, int d, in
                                : (float)Storage<S>::load(a.f1[Fd][gpos + sj], a.inv[Fd]);
           GhostAcc<S, false> A = ghost_acc<S, false>(a, ob);
           A.fd = Fd;
-          A.go[d] = side == 0 ? -1 : 0;
+          A.gd = d;
+          A.gv = side == 0 ? -1 : 0;
           A.ja = j;
           A.v0 = vg0;
           A.vn = vgn;
@@ -547,7 +550,7 @@ __device__ __forceinline__ void velocity_gen_block(const BcArgs<S> &a, int d, in
 // first also applies the source and advances the step counter, as
 // velocity_bc_merged_kernel.
 template <int R, typename S>
-__global__ void __launch_bounds__(256) velocity_bc_gen_kernel(BcArgs<S> a, S *txx, S *tyy, S *tzz, long src_off,
+__global__ void __launch_bounds__(256) velocity_bc_gen_kernel(const __grid_constant__ BcArgs<S> a, S *txx, S *tyy, S *tzz, long src_off,
                                                               const float *w, int nt, long *step, float s0, float s1,
                                                               float s2) {
   const int i2 = blockIdx.x * 32 + threadIdx.x, i1 = blockIdx.y * 8 + threadIdx.y;
@@ -714,13 +717,9 @@ __global__ void __launch_bounds__(128) stress_recompute_group_kernel(const Group
       if (a.face[2 * d + side] != 1) continue;
       const int fi = q < d ? q : q + 1;
       const int b = side == 0 ? m : nd - m - 1;
-      int c[3];
-      c[a1] = i1;
-      c[a2] = i2;
-      c[d] = b;
-      const auto A = ghost_acc<S, false>(a, lin(g, c[0], c[1], c[2]));
+      const auto A = ghost_acc<S, false>(a, plane_lin(g, d, i1, i2, b));
       const float v =
-          a.het ? GenGhost4<1>::stress(fi, d, side, A, a.kg) : GenGhost4<0>::stress(fi, d, side, A, a.kg);
+          gen_stress_recompute(a, fi, d, side, A);
       const_cast<float *>(a.rc)[(long)z * a.rcs + (long)i1 * n2 + i2] = v;
     }
   }

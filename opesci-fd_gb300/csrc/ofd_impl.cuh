@@ -47,10 +47,15 @@ struct DevState {
   int sr;              // 16-bit storage: stochastic rounding of the sweeps' stores
   int gen_ghost;       // space order 4: generated Levander ghost expressions (literals d_kg)
   float *d_kg;
+  int ghost_sd;        // the table d_kg allows the shared-divisor recompute (GenGhost4::stress_sd)
+  int sd_off;          // 1: evaluate the recompute term by term even so
   // precomputed normal-stress recompute values (generated ghosts): 12 planes
-  // of rcs floats, computed on stream st2 beside the stress sweep
+  // of rcs floats.  rc_mode 0: computed on the handle's stream after the
+  // stress sweep; 1: on stream st2 (highest priority) beside the sweep.
+  // rc_bps: blocks of 128 threads per SM of the recompute grid.
   float *d_rc;
   long rcs;
+  int rc_mode, rc_bps;
   cudaStream_t st2;
   cudaEvent_t ev_fork, ev_join;
   int nks, nkv;        // literal-table sizes (0 until ofd_set_coefficients)
@@ -88,6 +93,9 @@ struct Backend {
   // literal-table size of the generated ghost expressions (0: none for this
   // space order and storage)
   virtual int ghost_table_size(int het) const = 0;
+  // every shared-divisor recompute case of the table kg (host copy) has equal
+  // divisor literals in all its terms
+  virtual bool ghost_sd_ok(int het, const float *kg, int nkg) const = 0;
   // Grouped stepping: device tables of the members' arguments (all members
   // share this backend's space order and storage, and one media mode), and
   // one step of every member in 8 grouped launches.  chunk_planes: x chunk
@@ -120,6 +128,17 @@ inline int sm_count() {
     cache[dev] = n > 0 ? n : 152;
   }
   return cache[dev];
+}
+
+// Default schedule of the generated ghosts' recompute (ofd_set_ghost_schedule)
+#define OFD_RC_MODE_DEFAULT 1
+#define OFD_RC_BPS_DEFAULT 4
+
+// Numerically lowest (most urgent) stream priority of the current device.
+inline int greatest_priority() {
+  int least = 0, greatest = 0;
+  if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) return 0;
+  return greatest;
 }
 
 // ---- generic kernels ------------------------------------------------------
@@ -282,6 +301,7 @@ struct Impl : Backend {
     a.gen = (R == 2 && sizeof(S) <= 4 && s.gen_ghost && s.d_kg) ? 1 : 0;
     a.het = s.het;
     a.kg = s.d_kg;
+    a.gsd = s.ghost_sd && !s.sd_off;
     a.rc = nullptr;
     a.rcs = s.rcs;
     return a;
@@ -295,28 +315,46 @@ struct Impl : Backend {
     return dim3((n2 + 31) / 32, (n1 + 7) / 8, z);
   }
 
-  // The step's generated recompute values on the second stream, after the
-  // work already queued on st (the previous step's ghosts included), launched
-  // before the stress sweep with one 128-thread block per SM so that all of
-  // it is resident beside the sweep's two CTAs (its FP64 work beside the
-  // memory-bound sweep).  stress_bc waits for ev_join.
+  // The step's generated recompute values (12 face planes).  rc_mode 1: on
+  // the second stream after the work already queued on st (the previous
+  // step's ghosts included), launched before the stress sweep at the highest
+  // priority so that its blocks take the SM room the sweep's CTAs leave (its
+  // FP64 work beside the memory-bound sweep); stress_bc waits for ev_join.
+  // rc_mode 0: on st after the stress sweep.  The priority is a launch
+  // attribute, so graph capture keeps it.
   static bool pre_ok(const DevState &s) {
     return R == 2 && sizeof(S) <= 4 && s.gen_ghost && s.d_kg && s.d_rc && s.st2 && !s.legacy;
   }
-  void pre_fork(const DevState &s, cudaStream_t st) { cudaEventRecord(s.ev_fork, st); }
-  void pre_recompute(const DevState &s, int t1, int t0) {
+  void recompute_launch(const DevState &s, int t1, int t0, cudaStream_t st, int prio) {
     BcArgs<S> a = bc_args(s, t1, t0, 1);
-    cudaStreamWaitEvent(s.st2, s.ev_fork, 0);
     const Geom &g = s.g;
     const int nmax = std::max(g.n1, std::max(g.n2, g.n3));
-    stress_recompute_kernel<R, S><<<sm_count(), 128, 0, s.st2>>>(a, s.d_rc, nmax);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(sm_count() * std::max(1, s.rc_bps));
+    cfg.blockDim = dim3(128);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributePriority;
+    at[0].val.priority = prio;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, stress_recompute_kernel<R, S>, a, s.d_rc, nmax);
+  }
+  void pre_recompute(const DevState &s, int t1, int t0, cudaStream_t st) {
+    cudaEventRecord(s.ev_fork, st);
+    cudaStreamWaitEvent(s.st2, s.ev_fork, 0);
+    recompute_launch(s, t1, t0, s.st2, greatest_priority());
     cudaEventRecord(s.ev_join, s.st2);
   }
 
-  void stress_bc(const DevState &s, int t1, int t0, int recompute, cudaStream_t st, bool pre = false) {
+  // pre: the recompute values are in d_rc (beside: computed on st2, so wait
+  // for ev_join first)
+  void stress_bc(const DevState &s, int t1, int t0, int recompute, cudaStream_t st, bool pre = false,
+                 bool beside = false) {
     BcArgs<S> a = bc_args(s, t1, t0, recompute);
     if (pre) {
-      cudaStreamWaitEvent(st, s.ev_join, 0);
+      if (beside) cudaStreamWaitEvent(st, s.ev_join, 0);
       a.rc = s.d_rc;
     }
     for (int d = 0; d < 3; ++d) {
@@ -405,14 +443,13 @@ struct Impl : Backend {
     auto rec = [&](int i) { if (ev) cudaEventRecord(ev->ev[i], st); };
     rec(0);
     const bool pre = pre_ok(s);
-    if (pre) {
-      pre_fork(s, st);
-      pre_recompute(s, t1, t0);
-    }
+    const bool beside = pre && s.rc_mode == 1;
+    if (beside) pre_recompute(s, t1, t0, st);
     sweeps(s, t0, true, st);
     rec(1);
     rec(2);
-    stress_bc(s, t1, t0, s.legacy ? 0 : 1, st, pre);
+    if (pre && !beside) recompute_launch(s, t1, t0, st, 0);
+    stress_bc(s, t1, t0, s.legacy ? 0 : 1, st, pre, beside);
     rec(3);
     rec(4);
     sweeps(s, t0, false, st);
@@ -500,9 +537,9 @@ struct Impl : Backend {
     int sbc_blocks[3] = {0, 0, 0}, vbc_blocks[3] = {0, 0, 0};
     bool kd[2] = {false, false};   // [stress]: literal tables follow KMap (register-held literals)
     bool receivers = false;        // some member records traces
-    // generated-ghost recompute of the members that have it, on a second
-    // stream beside the stress sweep (as a single handle's step does)
-    int rc_blocks = 0;
+    // generated-ghost recompute of the members that have it, scheduled as
+    // the first member's rc_mode / rc_bps say (as a single handle's step)
+    int rc_blocks = 0, rc_mode = 0, rc_bps = 1;
     cudaStream_t st2 = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr;
     std::vector<void *> raw;   // allocations (tables start 128-byte aligned inside them)
@@ -594,6 +631,8 @@ struct Impl : Backend {
     pl->st = st;
     pl->n = n;
     pl->het = m[0]->het;
+    pl->rc_mode = m[0]->rc_mode;
+    pl->rc_bps = std::max(1, m[0]->rc_bps);
     if (pl->het) {
       pl->kd[1] = tables_follow_kmap<true>(m, n);
       pl->kd[0] = tables_follow_kmap<false>(m, n);
@@ -657,7 +696,7 @@ struct Impl : Backend {
       }
       pl->rc_blocks = rb;
       if (rb > 0 && !pl->st2) {
-        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&pl->st2, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&pl->st2, cudaStreamNonBlocking, greatest_priority());
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&pl->fork, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&pl->join, cudaEventDisableTiming);
       }
@@ -695,15 +734,30 @@ struct Impl : Backend {
       }
     };
     const bool pre = pl->rc_blocks > 0 && pl->st2;
-    if (pre) {
+    const bool beside = pre && pl->rc_mode == 1;
+    auto recompute = [&](cudaStream_t rs, int prio) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(std::min(pl->rc_blocks, sm_count() * pl->rc_bps));
+      cfg.blockDim = dim3(32, 4);
+      cfg.dynamicSmemBytes = 0;
+      cfg.stream = rs;
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributePriority;
+      at[0].val.priority = prio;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      cudaLaunchKernelEx(&cfg, stress_recompute_group_kernel<R, S>, (const GroupBc<S> *)pl->sbc[t0], n,
+                         pl->rc_blocks);
+    };
+    if (beside) {
       cudaEventRecord(pl->fork, st);
       cudaStreamWaitEvent(pl->st2, pl->fork, 0);
-      const int grid = std::min(pl->rc_blocks, sm_count());
-      stress_recompute_group_kernel<R, S><<<grid, dim3(32, 4), 0, pl->st2>>>(pl->sbc[t0], n, pl->rc_blocks);
+      recompute(pl->st2, greatest_priority());
       cudaEventRecord(pl->join, pl->st2);
     }
     sweep(true);
-    if (pre) cudaStreamWaitEvent(st, pl->join, 0);
+    if (beside) cudaStreamWaitEvent(st, pl->join, 0);
+    else if (pre) recompute(st, 0);
     for (int d = 0; d < 3; ++d)
       stress_bc_group_kernel<R, S><<<pl->sbc_blocks[d], dim3(32, 8), 0, st>>>(pl->sbc[t0], n, d);
     sweep(false);
@@ -722,6 +776,26 @@ struct Impl : Backend {
   int ghost_table_size(int het) const override {
     if constexpr (R == 2 && sizeof(S) <= 4) return het ? GenGhost4<1>::NK : GenGhost4<0>::NK;
     return 0;
+  }
+
+  bool ghost_sd_ok(int het, const float *kg, int nkg) const override {
+    if constexpr (R == 2 && sizeof(S) <= 4) {
+      const short *p = het ? GenGhost4<1>::SD_PAIRS : GenGhost4<0>::SD_PAIRS;
+      const int n = het ? GenGhost4<1>::SD_N : GenGhost4<0>::SD_N;
+      // groups: key, term count, then (a, b) per term
+      for (int i = 0; i + 1 < n;) {
+        const int terms = p[i + 1];
+        const short *ab = p + i + 2;
+        if (i + 2 + 2 * terms > n) return false;
+        for (int t = 0; t < 2 * terms; ++t)
+          if (ab[t] < 0 || ab[t] >= nkg) return false;
+        for (int t = 1; t < terms; ++t)
+          if (kg[ab[2 * t]] != kg[ab[0]] || kg[ab[2 * t + 1]] != kg[ab[1]]) return false;
+        i += 2 + 2 * terms;
+      }
+      return true;
+    }
+    return false;
   }
 
   int table_size(int het, int stress) const override {

@@ -138,6 +138,48 @@ def _variant_grid(space_order, hetero):
                         analytic=False, free_surface=False)
 
 
+def split_terms(expr):
+    """The top-level terms of a printed sum, left to right: [(op, term)] with
+    op '' for the first term (which may carry a unary sign) and '+'/'-' for
+    the rest.  Rejoining them gives the expression back exactly."""
+    out, depth, start, op = [], 0, 0, ''
+    i = 0
+    while i < len(expr):
+        c = expr[i]
+        if c in '([':
+            depth += 1
+        elif c in ')]':
+            depth -= 1
+        elif depth == 0 and expr[i:i + 3] in (' + ', ' - ') and i > start:
+            out.append((op, expr[start:i]))
+            op = expr[i + 1]
+            start = i + 3
+            i += 3
+            continue
+        i += 1
+    out.append((op, expr[start:]))
+    back = out[0][1] + ''.join(' %s %s' % (o, t) for o, t in out[1:])
+    if back != expr:
+        raise RuntimeError('term split does not reproduce the expression')
+    return out
+
+
+def interleaved_lines(exprs, indent='    '):
+    """Statements evaluating the sums ``exprs`` into out[0..n-1] with their
+    accumulation chains interleaved term by term: chain i is still
+    ((t0 op t1) op t2) ... in its printed order, so every result rounds
+    exactly as the single expression does, while the independent chains sit
+    side by side for the instruction scheduler."""
+    terms = [split_terms(e) for e in exprs]
+    lines = ['%sC o%d = %s;' % (indent, i, t[0][1]) for i, t in enumerate(terms)]
+    for k in range(1, max(len(t) for t in terms)):
+        for i, t in enumerate(terms):
+            if k < len(t):
+                lines.append('%so%d = o%d %s %s;' % (indent, i, i, t[k][0], t[k][1]))
+    lines += ['%sout[%d] = o%d;' % (indent, i, i) for i in range(len(terms))]
+    return lines
+
+
 def generate_headers(outdir):
     """Write sweeps_gen.cuh and signatures.json for all prebuilt variants."""
     os.makedirs(outdir, exist_ok=True)
@@ -145,7 +187,8 @@ def generate_headers(outdir):
     lines = ['// GENERATED by opesci/templates/cuda_gen.py from the symbolic kernels of',
              '// StaggeredGrid (expanded, constant-folded, media resolved); do not edit.',
              '// Each function evaluates the reference generator\'s C expression of the',
-             '// update with its literals taken from the table K.',
+             '// update with its literals taken from the table K, the sums of the',
+             '// outputs interleaved term by term (each in its printed order).',
              '#pragma once', '#include "ofd_common.cuh"', '', 'namespace ofd {', '',
              'template <int R, int HET> struct GenSweep { static constexpr bool ok = false; };', '']
     for so in (2, 4, 6, 8):
@@ -171,13 +214,11 @@ def generate_headers(outdir):
             lines.append('  static constexpr int NK_STRESS = %d, NK_VELOCITY = %d;' % (len(sl), len(vl)))
             lines.append('  template <typename C, class Acc, class KT>')
             lines.append('  __device__ __forceinline__ static void stress(const Acc &A, const KT &K, C out[6]) {')
-            for i, e in enumerate(se):
-                lines.append('    out[%d] = %s;' % (i, e))
+            lines += interleaved_lines(se)
             lines.append('  }')
             lines.append('  template <typename C, class Acc, class KT>')
             lines.append('  __device__ __forceinline__ static void velocity(const Acc &A, const KT &K, C out[3]) {')
-            for i, e in enumerate(ve):
-                lines.append('    out[%d] = %s;' % (i, e))
+            lines += interleaved_lines(ve)
             lines.append('  }')
             lines.append('};')
             lines.append('')
@@ -361,6 +402,36 @@ def _ghost_variant_grid(hetero):
                         analytic=False, free_surface=True)
 
 
+_GDEN = re.compile(r'^(.*)/\((K\[(\d+)\]\*(A\.m\([^()]*\)) \+ K\[(\d+)\]\*(A\.m\([^()]*\)))\)$')
+
+
+def shared_divisor_case(text):
+    """A ghost expression whose every top-level term ends in a division by
+    (K[a]*M1 + K[b]*M2) with the same media references M1, M2: returns
+    (divisor text with the first term's literals, the expression with each
+    division replaced, [(a, b)] per term), else None.  A float term NUM/(den)
+    becomes (NUM)/Dq, a double term (one holding ofd_pow2) q.div(NUM); both
+    round exactly as the original when the runtime has checked that every
+    term's (K[a], K[b]) equal the first term's."""
+    terms = split_terms(text)
+    pairs, media, out = [], None, []
+    for op, t in terms:
+        m = _GDEN.match(t)
+        if not m:
+            return None
+        num, a, m1, b, m2 = m.group(1), int(m.group(3)), m.group(4), int(m.group(5)), m.group(6)
+        if media is None:
+            media = (m1, m2)
+        elif media != (m1, m2):
+            return None
+        pairs.append((a, b))
+        rep = 'q.div(%s)' % num if 'ofd_pow2' in num else '(%s)/Dq' % num
+        out.append((op, rep))
+    den = 'K[%d]*%s + K[%d]*%s' % (pairs[0][0], media[0], pairs[0][1], media[1])
+    body = out[0][1] + ''.join(' %s %s' % (o, t) for o, t in out[1:])
+    return den, body, pairs
+
+
 def generate_ghost_header(outdir, sigs):
     """ghosts_gen.cuh: GenGhost4<HET>::stress / ::velocity, and the ghost
     signatures into ``sigs`` (so4_het / so4_const: 'ghost', 'nk_ghost')."""
@@ -370,7 +441,8 @@ def generate_ghost_header(outdir, sigs):
              '// expression of one ghost value with its literals taken from the table K;',
              '// A(F, level, ox, oy, oz) is the field at level t0 (0) or t1 (1) at an offset',
              '// from the ghost row\'s point on the boundary plane, A.m(M, ox, oy, oz) a medium.',
-             '#pragma once', '#include "ofd_common.cuh"', '', 'namespace ofd {', '',
+             '#pragma once', '#include "ofd_common.cuh"', '#include "ofd_shared_div.cuh"', '',
+             'namespace ofd {', '',
              '// the exact double square of a float (pow(float, 2) of the reference\'s C++)',
              '__device__ __forceinline__ double ofd_pow2(float v) { return (double)v * (double)v; }', '',
              'template <int HET> struct GenGhost4 { static constexpr bool ok = false; };', '']
@@ -387,7 +459,7 @@ def generate_ghost_header(outdir, sigs):
             lines.append('  // %s ghost of component c on face normal d, side (0 lower, 1 upper)' %
                          ('normal-stress recompute' if kind == 'stress' else 'velocity'))
             lines.append('  template <class Acc, class KT>')
-            lines.append('  __device__ static float %s(int c, int d, int side, const Acc &A, const KT &K) {' % kind)
+            lines.append('  __device__ %sstatic float %s(int c, int d, int side, const Acc &A, const KT &K) {' % ('__forceinline__ ' if kind == 'velocity' else '', kind))
             lines.append('    switch (c * 6 + d * 2 + side) {')
             for k, c, d, side, t in cases:
                 if k == kind:
@@ -395,6 +467,33 @@ def generate_ghost_header(outdir, sigs):
             lines.append('    }')
             lines.append('    return 0.f;')
             lines.append('  }')
+        sd = [(c * 6 + d * 2 + side, shared_divisor_case(t)) for k, c, d, side, t in cases if k == 'stress']
+        sd = [(key, r) for key, r in sd if r is not None]
+        lines.append('  // normal-stress recompute with the common divisor of each case\'s terms')
+        lines.append('  // formed once: float quotients divide by it, double quotients go through')
+        lines.append('  // SharedDiv.  Exact only when every term\'s divisor literals equal the')
+        lines.append('  // first term\'s (SD_PAIRS; the runtime checks the table); other cases')
+        lines.append('  // evaluate as stress().')
+        lines.append('  template <class Acc, class KT>')
+        lines.append('  __device__ static float stress_sd(int c, int d, int side, const Acc &A, const KT &K) {')
+        if sd:
+            lines.append('    switch (c * 6 + d * 2 + side) {')
+            for key, (den, body, _) in sd:
+                lines.append('      case %d: {' % key)
+                lines.append('        const float Dq = %s;' % den)
+                lines.append('        const SharedDiv q(Dq);')
+                lines.append('        return (float)(%s);' % body)
+                lines.append('      }')
+            lines.append('    }')
+        lines.append('    return stress(c, d, side, A, K);')
+        lines.append('  }')
+        flat = []
+        for key, (_, _, pairs) in sd:
+            flat += [key, len(pairs)] + [v for ab in pairs for v in ab]
+        lines.append('  // per shared-divisor case: key, term count, then (a, b) literal indices per term')
+        lines.append('  static constexpr int SD_N = %d;' % len(flat))
+        lines.append('  static constexpr short SD_PAIRS[%d] = {%s};' % (max(1, len(flat)),
+                                                                  ', '.join(str(v) for v in flat) or '0'))
         lines.append('};')
         lines.append('')
     lines.append('}  // namespace ofd')

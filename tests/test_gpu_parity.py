@@ -139,7 +139,7 @@ FACE_MIXES = {
 }
 
 
-def run_random_state(so, n, faces, storage, mode, steps=6):
+def run_random_state(so, n, faces, storage, mode, steps=6, schedule=None):
     """Layered media, random initial fields everywhere (so every ghost and
     recompute path sees non-zero data), ``steps`` steps.  mode: 'tiled',
     'plain' (kernel variant 1) or 'persistent'.  A storage name ending in
@@ -162,6 +162,8 @@ def run_random_state(so, n, faces, storage, mode, steps=6):
     for f in runtime.FIELDS:
         sim.upload(f, 0, rng.standard_normal(tuple(cfg.dim)).astype(np.float32) * (1e-7 if f in 'UVW' else 1.0))
     sim.boundary_init(0)
+    if schedule is not None:
+        sim.set_ghost_schedule(*schedule)
     if mode == 'persistent':
         sim.set_persistent(1)
         sim.step_graph(steps)
@@ -195,6 +197,26 @@ def test_boundary_paths_identical_across_kernels(so, n, faces, storage):
         assert np.array_equal(a[f], b[f]), ('tiled/plain', f)
         assert np.array_equal(b[f], c[f]), ('plain/persistent', f)
         assert np.array_equal(a[f], e[f]), ('steps/graph', f)
+
+
+@pytest.mark.parametrize('storage', ['f32', 'f16'])
+def test_ghost_schedules_identical(storage):
+    """The generated space-order-4 ghosts' recompute after the stress sweep
+    or beside it on the second stream, with any grid size, launched or
+    replayed from graphs, shared-divisor or term-by-term evaluation:
+    bit-identical results."""
+    runs = [run_random_state(4, 72, FACE_MIXES['levander'], storage, mode, schedule=sch)
+            for mode, sch in (('tiled', (1, 4, 1)), ('tiled', (0, 4, 0)), ('graph', (0, 16, 1)), ('graph', (1, 1, 0)))]
+    for r in runs[1:]:
+        for f in runtime.FIELDS:
+            assert np.array_equal(runs[0][f], r[f]), f
+
+
+def test_shared_division_equals_ieee_division():
+    """The shared-divisor FP64 quotient (reciprocal, then remainder
+    corrections) against CUDA's IEEE division on 2^26 seeded operand pairs,
+    a third of them with quotients next to a rounding midpoint."""
+    assert runtime.check_shared_division(1 << 26, seed=7) == 0
 
 
 def test_tiled_constant_media_identical():
