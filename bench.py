@@ -217,7 +217,8 @@ def elastic_e2e(sim, media, src, wav, steps, lups):
     """One job through the C ABI as a user runs it: media from pinned host
     memory in (with the effective-media preprocessing), ``steps`` steps, the
     nine final fields out to pinned host memory, all in the timed region (one
-    wait at the end).  A second, phase-timed pass gives the transfer rates,
+    wait at the end).  After one warm-up job, the median of three jobs is
+    the value; a phase-timed job after them gives the transfer rates,
     against the plain copy bandwidth of the host link."""
     import numpy as np
     import torch
@@ -254,11 +255,14 @@ def elastic_e2e(sim, media, src, wav, steps, lups):
             phases['download_s'] = t2 - t1
         return t2 - t0
 
-    wall = job(steps)
+    job(steps)   # warm-up: first DMA use of the pinned buffers, the library's scratch pool
+    walls = sorted(job(steps) for _ in range(3))
+    wall = walls[1]
     phases = {}
     job(steps, phases)
     link = link_bandwidth(int(cells) * 4)
     return {'value': lups / wall / 1e9, 'unit': UNIT,
+            'jobs_s': walls,
             'h2d_bytes_per_step': (3 * cells * 4 + len(wav) * 4) / steps,
             'd2h_bytes_per_step': 9 * cells * 4 / steps,
             'seconds': wall,
@@ -267,8 +271,9 @@ def elastic_e2e(sim, media, src, wav, steps, lups):
             'field_download_GBps': 9 * cells * 4 / phases['download_s'] / 1e9,
             'link_GBps': link,
             'note': 'one job through the C ABI from pinned host buffers: media upload + effective media, '
-                    'K steps, download of the 9 final fields (one wait at the end); media_upload_GBps '
-                    'includes the effective-media preprocessing; link_GBps is a plain pinned copy'}
+                    'K steps, download of the 9 final fields (one wait at the end); median of 3 jobs after '
+                    'a warm-up job; media_upload_GBps includes the effective-media preprocessing; '
+                    'link_GBps is a plain pinned copy'}
 
 
 def run_reference(args, rank):

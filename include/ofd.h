@@ -208,18 +208,9 @@ int ofd_set_wait_limit(ofd_handle *h, double seconds);
  * loops): mode 0 runs it on the handle's stream after the stress sweep,
  * mode 1 (default) on a second stream at the highest priority beside the
  * stress sweep (ofd_set_ghost_coefficients creates that stream);
- * blocks_per_sm in [1, 16] sizes its grid (128-thread blocks).
- * shared_divisor 1 (default) evaluates each recompute case with its common
- * divisor formed once and FP64 quotients by reciprocal and remainder
- * correction (when ofd_set_ghost_coefficients found the table's divisor
- * literals equal), 0 term by term as printed.  Results are identical in
- * every setting.  Cached graphs are rebuilt. */
-int ofd_set_ghost_schedule(ofd_handle *h, int mode, int blocks_per_sm, int shared_divisor);
-/* Self-check of the shared-divisor FP64 quotient (no counterpart in the
- * reference): n seeded operand pairs (random, near-exact and near-midpoint
- * quotients) divided on the current device both ways; *mismatches receives
- * how many results differ from the IEEE division x / D. */
-int ofd_check_shared_division(long n, unsigned long long seed, long *mismatches);
+ * blocks_per_sm in [1, 16] (default 4) sizes its grid (128-thread blocks).
+ * Results are identical in every setting.  Cached graphs are rebuilt. */
+int ofd_set_ghost_schedule(ofd_handle *h, int mode, int blocks_per_sm);
 /* Persistent time stepping (no counterpart in the reference): when enabled,
  * ofd_step and ofd_step_graph run up to 1024 whole steps per cooperative
  * launch, with grid barriers between the phases of a step.  For small grids,

@@ -129,9 +129,7 @@ __device__ __forceinline__ float gen_velocity_ghost(const BcArgs<S> &a, int c, i
 // generated normal-stress recompute value of stress fi on face (d, side)
 template <class Acc, class S>
 __device__ __forceinline__ float gen_stress_recompute(const BcArgs<S> &a, int fi, int d, int side, const Acc &A) {
-  if (a.het)
-    return a.gsd ? GenGhost4<1>::stress_sd(fi, d, side, A, a.kg) : GenGhost4<1>::stress(fi, d, side, A, a.kg);
-  return a.gsd ? GenGhost4<0>::stress_sd(fi, d, side, A, a.kg) : GenGhost4<0>::stress(fi, d, side, A, a.kg);
+  return a.het ? GenGhost4<1>::stress(fi, d, side, A, a.kg) : GenGhost4<0>::stress(fi, d, side, A, a.kg);
 }
 
 // Stress ghosts of face normal d at in-plane point (i1, i2) for stress
@@ -220,8 +218,11 @@ __device__ __forceinline__ void stress_bc_point(const BcArgs<S> &a, int d, int i
 // each sum double) then use the FP64 units the memory-bound sweep leaves
 // idle.  Grid-stride over virtual 32 x 4 tiles of the 12 face planes (lane:
 // i2, warp: i1), so that a small grid of a few blocks per SM covers it.
+// At most 40 registers a thread: two space-order-4 sweep CTAs (288 threads
+// x 96 registers each) leave 10,240 registers of an SM, room for two such
+// blocks beside them.
 template <int R, typename S>
-__global__ void __launch_bounds__(128) stress_recompute_kernel(const __grid_constant__ BcArgs<S> a, float *rc, int nmax) {
+__global__ void __launch_bounds__(128, 12) stress_recompute_kernel(const __grid_constant__ BcArgs<S> a, float *rc, int nmax) {
   if constexpr (R == 2 && sizeof(S) <= 4) {
     const Geom &g = a.g;
     const int m = g.m;

@@ -158,9 +158,6 @@ template <typename S> struct BcArgs {
   // formulas
   int gen, het;
   const float *kg;
-  // 1: every generated recompute case has one divisor literal pair (checked on
-  // the host), so the shared-divisor form GenGhost4::stress_sd applies
-  int gsd;
   // normal-stress recompute values precomputed for this step (stress ghosts
   // with gen): rc[((d * 2 + side) * 2 + q) * rcs + i1 * n2(d) + i2], q the
   // index of the recomputed normal stress among the two of face normal d;

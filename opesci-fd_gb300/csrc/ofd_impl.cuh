@@ -47,8 +47,6 @@ struct DevState {
   int sr;              // 16-bit storage: stochastic rounding of the sweeps' stores
   int gen_ghost;       // space order 4: generated Levander ghost expressions (literals d_kg)
   float *d_kg;
-  int ghost_sd;        // the table d_kg allows the shared-divisor recompute (GenGhost4::stress_sd)
-  int sd_off;          // 1: evaluate the recompute term by term even so
   // precomputed normal-stress recompute values (generated ghosts): 12 planes
   // of rcs floats.  rc_mode 0: computed on the handle's stream after the
   // stress sweep; 1: on stream st2 (highest priority) beside the sweep.
@@ -93,9 +91,6 @@ struct Backend {
   // literal-table size of the generated ghost expressions (0: none for this
   // space order and storage)
   virtual int ghost_table_size(int het) const = 0;
-  // every shared-divisor recompute case of the table kg (host copy) has equal
-  // divisor literals in all its terms
-  virtual bool ghost_sd_ok(int het, const float *kg, int nkg) const = 0;
   // Grouped stepping: device tables of the members' arguments (all members
   // share this backend's space order and storage, and one media mode), and
   // one step of every member in 8 grouped launches.  chunk_planes: x chunk
@@ -301,7 +296,6 @@ struct Impl : Backend {
     a.gen = (R == 2 && sizeof(S) <= 4 && s.gen_ghost && s.d_kg) ? 1 : 0;
     a.het = s.het;
     a.kg = s.d_kg;
-    a.gsd = s.ghost_sd && !s.sd_off;
     a.rc = nullptr;
     a.rcs = s.rcs;
     return a;
@@ -776,26 +770,6 @@ struct Impl : Backend {
   int ghost_table_size(int het) const override {
     if constexpr (R == 2 && sizeof(S) <= 4) return het ? GenGhost4<1>::NK : GenGhost4<0>::NK;
     return 0;
-  }
-
-  bool ghost_sd_ok(int het, const float *kg, int nkg) const override {
-    if constexpr (R == 2 && sizeof(S) <= 4) {
-      const short *p = het ? GenGhost4<1>::SD_PAIRS : GenGhost4<0>::SD_PAIRS;
-      const int n = het ? GenGhost4<1>::SD_N : GenGhost4<0>::SD_N;
-      // groups: key, term count, then (a, b) per term
-      for (int i = 0; i + 1 < n;) {
-        const int terms = p[i + 1];
-        const short *ab = p + i + 2;
-        if (i + 2 + 2 * terms > n) return false;
-        for (int t = 0; t < 2 * terms; ++t)
-          if (ab[t] < 0 || ab[t] >= nkg) return false;
-        for (int t = 1; t < terms; ++t)
-          if (kg[ab[2 * t]] != kg[ab[0]] || kg[ab[2 * t + 1]] != kg[ab[1]]) return false;
-        i += 2 + 2 * terms;
-      }
-      return true;
-    }
-    return false;
   }
 
   int table_size(int het, int stress) const override {

@@ -412,8 +412,6 @@ int ofd_create(const ofd_config *cfg, ofd_handle **out) {
   h->s.rcs = 0;
   h->s.st2 = nullptr;
   h->s.ev_fork = h->s.ev_join = nullptr;
-  h->s.ghost_sd = 0;
-  h->s.sd_off = 0;
   h->s.rc_mode = OFD_RC_MODE_DEFAULT;
   h->s.rc_bps = OFD_RC_BPS_DEFAULT;
   h->s.dt = cfg->dt;
@@ -535,7 +533,6 @@ int ofd_set_ghost_coefficients(ofd_handle *h, int het, const float *kg, int nkg)
   OFD_CUDA(cudaMemcpyAsync(h->s.d_kg, kg, sizeof(float) * (size_t)nkg, cudaMemcpyHostToDevice, h->stream));
   OFD_CUDA(cudaStreamSynchronize(h->stream));
   h->s.gen_ghost = 1;
-  h->s.ghost_sd = h->be->ghost_sd_ok(het, kg, nkg) ? 1 : 0;
   drop_graphs(h);
   return OFD_OK;
 }
@@ -893,14 +890,12 @@ int ofd_set_wait_limit(ofd_handle *h, double seconds) {
   return OFD_OK;
 }
 
-int ofd_set_ghost_schedule(ofd_handle *h, int mode, int blocks_per_sm, int shared_divisor) {
+int ofd_set_ghost_schedule(ofd_handle *h, int mode, int blocks_per_sm) {
   if (!h) return fail(OFD_EINVAL, "null handle");
   if (mode != 0 && mode != 1) return fail(OFD_EINVAL, "ghost schedule mode must be 0 (after the sweep) or 1 (beside it)");
   if (blocks_per_sm < 1 || blocks_per_sm > 16) return fail(OFD_EINVAL, "blocks_per_sm must be in [1, 16]");
-  if (shared_divisor != 0 && shared_divisor != 1) return fail(OFD_EINVAL, "shared_divisor must be 0 or 1");
   h->s.rc_mode = mode;
   h->s.rc_bps = blocks_per_sm;
-  h->s.sd_off = shared_divisor ? 0 : 1;
   drop_graphs(h);
   return OFD_OK;
 }

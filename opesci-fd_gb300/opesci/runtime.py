@@ -102,8 +102,7 @@ def load_library():
         'ofd_step_graph': [h, ctypes.c_int],
         'ofd_set_persistent': [h, ctypes.c_int],
         'ofd_set_wait_limit': [h, ctypes.c_double],
-        'ofd_set_ghost_schedule': [h, ctypes.c_int, ctypes.c_int, ctypes.c_int],
-        'ofd_check_shared_division': [ctypes.c_long, ctypes.c_ulonglong, P(ctypes.c_long)],
+        'ofd_set_ghost_schedule': [h, ctypes.c_int, ctypes.c_int],
         'ofd_step_timed': [h, ctypes.c_int, P(ctypes.c_double), P(ctypes.c_long)],
         'ofd_set_tuning': [h, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int],
         'ofd_step_profiled': [h, ctypes.c_int, P(ctypes.c_double), P(ctypes.c_double), P(ctypes.c_long)],
@@ -159,15 +158,6 @@ def set_device(index):
     GPU passes its local rank)."""
     lib = load_library()
     _check(lib.ofd_set_device(int(index)), 'ofd_set_device')
-
-
-def check_shared_division(n, seed=1):
-    """Run the device self-check of the shared-divisor FP64 quotient on n
-    seeded operand pairs; returns how many differ from IEEE x / D."""
-    lib = load_library()
-    bad = ctypes.c_long()
-    _check(lib.ofd_check_shared_division(int(n), int(seed), ctypes.byref(bad)), 'ofd_check_shared_division')
-    return bad.value
 
 
 def _check(rc, what):
@@ -407,13 +397,11 @@ class Simulation(object):
         OFDError with code OFD_ETIMEOUT."""
         _check(self.lib.ofd_set_wait_limit(self.h, float(seconds)), 'ofd_set_wait_limit')
 
-    def set_ghost_schedule(self, mode, blocks_per_sm, shared_divisor=1):
+    def set_ghost_schedule(self, mode, blocks_per_sm):
         """Where the generated space-order-4 ghosts' recompute runs: mode 0
         after the stress sweep, 1 beside it on a high-priority stream;
-        blocks_per_sm sizes its grid; shared_divisor 0 evaluates it term by
-        term.  Results do not depend on any of them."""
-        _check(self.lib.ofd_set_ghost_schedule(self.h, int(mode), int(blocks_per_sm), int(shared_divisor)),
-               'ofd_set_ghost_schedule')
+        blocks_per_sm sizes its grid.  Results do not depend on either."""
+        _check(self.lib.ofd_set_ghost_schedule(self.h, int(mode), int(blocks_per_sm)), 'ofd_set_ghost_schedule')
 
     def set_tuning(self, stress_variant=0, velocity_variant=0, chunk_waves=1, plain_bx=32, plain_by=8,
                    persistent=0):

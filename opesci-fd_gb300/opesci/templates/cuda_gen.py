@@ -180,6 +180,18 @@ def interleaved_lines(exprs, indent='    '):
     return lines
 
 
+def sequential_lines(exprs, indent='    '):
+    """One statement per output, each sum as printed."""
+    return ['%sout[%d] = %s;' % (indent, i, e) for i, e in enumerate(exprs)]
+
+
+# Space orders whose sweeps are emitted with interleaved chains: measured on
+# the GB300 at 512^3, interleaving shortened the space-order-4 velocity sweep
+# (1.331 -> 1.315 ms) and lengthened the space-order-8 sweeps (2.45 -> 2.53 ms
+# stress, 2.00 -> 2.09 ms velocity), whose long chains already overlap.
+INTERLEAVE_MAX_ORDER = 4
+
+
 def generate_headers(outdir):
     """Write sweeps_gen.cuh and signatures.json for all prebuilt variants."""
     os.makedirs(outdir, exist_ok=True)
@@ -187,8 +199,9 @@ def generate_headers(outdir):
     lines = ['// GENERATED by opesci/templates/cuda_gen.py from the symbolic kernels of',
              '// StaggeredGrid (expanded, constant-folded, media resolved); do not edit.',
              '// Each function evaluates the reference generator\'s C expression of the',
-             '// update with its literals taken from the table K, the sums of the',
-             '// outputs interleaved term by term (each in its printed order).',
+             '// update with its literals taken from the table K; up to space order 4',
+             '// the sums of the outputs are interleaved term by term (each chain in',
+             '// its printed order).',
              '#pragma once', '#include "ofd_common.cuh"', '', 'namespace ofd {', '',
              'template <int R, int HET> struct GenSweep { static constexpr bool ok = false; };', '']
     for so in (2, 4, 6, 8):
@@ -214,11 +227,11 @@ def generate_headers(outdir):
             lines.append('  static constexpr int NK_STRESS = %d, NK_VELOCITY = %d;' % (len(sl), len(vl)))
             lines.append('  template <typename C, class Acc, class KT>')
             lines.append('  __device__ __forceinline__ static void stress(const Acc &A, const KT &K, C out[6]) {')
-            lines += interleaved_lines(se)
+            lines += interleaved_lines(se) if so <= INTERLEAVE_MAX_ORDER else sequential_lines(se)
             lines.append('  }')
             lines.append('  template <typename C, class Acc, class KT>')
             lines.append('  __device__ __forceinline__ static void velocity(const Acc &A, const KT &K, C out[3]) {')
-            lines += interleaved_lines(ve)
+            lines += interleaved_lines(ve) if so <= INTERLEAVE_MAX_ORDER else sequential_lines(ve)
             lines.append('  }')
             lines.append('};')
             lines.append('')
@@ -402,36 +415,6 @@ def _ghost_variant_grid(hetero):
                         analytic=False, free_surface=True)
 
 
-_GDEN = re.compile(r'^(.*)/\((K\[(\d+)\]\*(A\.m\([^()]*\)) \+ K\[(\d+)\]\*(A\.m\([^()]*\)))\)$')
-
-
-def shared_divisor_case(text):
-    """A ghost expression whose every top-level term ends in a division by
-    (K[a]*M1 + K[b]*M2) with the same media references M1, M2: returns
-    (divisor text with the first term's literals, the expression with each
-    division replaced, [(a, b)] per term), else None.  A float term NUM/(den)
-    becomes (NUM)/Dq, a double term (one holding ofd_pow2) q.div(NUM); both
-    round exactly as the original when the runtime has checked that every
-    term's (K[a], K[b]) equal the first term's."""
-    terms = split_terms(text)
-    pairs, media, out = [], None, []
-    for op, t in terms:
-        m = _GDEN.match(t)
-        if not m:
-            return None
-        num, a, m1, b, m2 = m.group(1), int(m.group(3)), m.group(4), int(m.group(5)), m.group(6)
-        if media is None:
-            media = (m1, m2)
-        elif media != (m1, m2):
-            return None
-        pairs.append((a, b))
-        rep = 'q.div(%s)' % num if 'ofd_pow2' in num else '(%s)/Dq' % num
-        out.append((op, rep))
-    den = 'K[%d]*%s + K[%d]*%s' % (pairs[0][0], media[0], pairs[0][1], media[1])
-    body = out[0][1] + ''.join(' %s %s' % (o, t) for o, t in out[1:])
-    return den, body, pairs
-
-
 def generate_ghost_header(outdir, sigs):
     """ghosts_gen.cuh: GenGhost4<HET>::stress / ::velocity, and the ghost
     signatures into ``sigs`` (so4_het / so4_const: 'ghost', 'nk_ghost')."""
@@ -441,8 +424,7 @@ def generate_ghost_header(outdir, sigs):
              '// expression of one ghost value with its literals taken from the table K;',
              '// A(F, level, ox, oy, oz) is the field at level t0 (0) or t1 (1) at an offset',
              '// from the ghost row\'s point on the boundary plane, A.m(M, ox, oy, oz) a medium.',
-             '#pragma once', '#include "ofd_common.cuh"', '#include "ofd_shared_div.cuh"', '',
-             'namespace ofd {', '',
+             '#pragma once', '#include "ofd_common.cuh"', '', 'namespace ofd {', '',
              '// the exact double square of a float (pow(float, 2) of the reference\'s C++)',
              '__device__ __forceinline__ double ofd_pow2(float v) { return (double)v * (double)v; }', '',
              'template <int HET> struct GenGhost4 { static constexpr bool ok = false; };', '']
@@ -467,33 +449,6 @@ def generate_ghost_header(outdir, sigs):
             lines.append('    }')
             lines.append('    return 0.f;')
             lines.append('  }')
-        sd = [(c * 6 + d * 2 + side, shared_divisor_case(t)) for k, c, d, side, t in cases if k == 'stress']
-        sd = [(key, r) for key, r in sd if r is not None]
-        lines.append('  // normal-stress recompute with the common divisor of each case\'s terms')
-        lines.append('  // formed once: float quotients divide by it, double quotients go through')
-        lines.append('  // SharedDiv.  Exact only when every term\'s divisor literals equal the')
-        lines.append('  // first term\'s (SD_PAIRS; the runtime checks the table); other cases')
-        lines.append('  // evaluate as stress().')
-        lines.append('  template <class Acc, class KT>')
-        lines.append('  __device__ static float stress_sd(int c, int d, int side, const Acc &A, const KT &K) {')
-        if sd:
-            lines.append('    switch (c * 6 + d * 2 + side) {')
-            for key, (den, body, _) in sd:
-                lines.append('      case %d: {' % key)
-                lines.append('        const float Dq = %s;' % den)
-                lines.append('        const SharedDiv q(Dq);')
-                lines.append('        return (float)(%s);' % body)
-                lines.append('      }')
-            lines.append('    }')
-        lines.append('    return stress(c, d, side, A, K);')
-        lines.append('  }')
-        flat = []
-        for key, (_, _, pairs) in sd:
-            flat += [key, len(pairs)] + [v for ab in pairs for v in ab]
-        lines.append('  // per shared-divisor case: key, term count, then (a, b) literal indices per term')
-        lines.append('  static constexpr int SD_N = %d;' % len(flat))
-        lines.append('  static constexpr short SD_PAIRS[%d] = {%s};' % (max(1, len(flat)),
-                                                                  ', '.join(str(v) for v in flat) or '0'))
         lines.append('};')
         lines.append('')
     lines.append('}  // namespace ofd')

@@ -203,20 +203,12 @@ def test_boundary_paths_identical_across_kernels(so, n, faces, storage):
 def test_ghost_schedules_identical(storage):
     """The generated space-order-4 ghosts' recompute after the stress sweep
     or beside it on the second stream, with any grid size, launched or
-    replayed from graphs, shared-divisor or term-by-term evaluation:
-    bit-identical results."""
+    replayed from graphs: bit-identical results."""
     runs = [run_random_state(4, 72, FACE_MIXES['levander'], storage, mode, schedule=sch)
-            for mode, sch in (('tiled', (1, 4, 1)), ('tiled', (0, 4, 0)), ('graph', (0, 16, 1)), ('graph', (1, 1, 0)))]
+            for mode, sch in (('tiled', (1, 4)), ('tiled', (0, 4)), ('graph', (0, 16)), ('graph', (1, 1)))]
     for r in runs[1:]:
         for f in runtime.FIELDS:
             assert np.array_equal(runs[0][f], r[f]), f
-
-
-def test_shared_division_equals_ieee_division():
-    """The shared-divisor FP64 quotient (reciprocal, then remainder
-    corrections) against CUDA's IEEE division on 2^26 seeded operand pairs,
-    a third of them with quotients next to a rounding midpoint."""
-    assert runtime.check_shared_division(1 << 26, seed=7) == 0
 
 
 def test_tiled_constant_media_identical():

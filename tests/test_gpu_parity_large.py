@@ -9,9 +9,10 @@ chunks per tile column, so the TMA ring geometry, the chunk boundaries and
 the grid of several waves are all exercised, which the small parity cases do
 not reach.
 
-Tolerance: every field within 1e-5 relative L2 of its own norm after the run
-(FP32).  Space order 8 (Robertsson ghosts: exact zeros and mirrors) is
-bit-identical to the oracle.  The oracle is built with vectorisation on
+Every field must be bit-identical to the oracle's at both orders (the
+printed update and ghost expressions evaluated in the reference's term
+order and types); the 1e-5 relative L2 bound is checked first so that a
+failure reports its size.  The oracle is built with vectorisation on
 (-O3 -fopenmp -ffp-contract=off): elementwise loops vectorise without any
 change to the IEEE operations, so its results equal the scalar build's and it
 finishes in about half the time.
@@ -62,8 +63,7 @@ def test_512_heterogeneous_source_matches_oracle(tmp_path, so):
     print('512^3 SO%d, 100 steps: relative L2 vs oracle' % so, {k: '%.2e' % v for k, v in errs.items()},
           'bit-identical fields:', [k for k, v in same.items() if v])
     assert max(errs.values()) < TOL, errs
-    if so == 8:
-        assert all(same.values()), same
+    assert all(same.values()), same
 
 
 @pytest.mark.skipif(os.environ.get('OFD_RUN_SLOW') != '1', reason='opt-in: OFD_RUN_SLOW=1 (full 1000-step run)')
@@ -71,3 +71,4 @@ def test_512_so4_full_run_matches_oracle(tmp_path):
     errs, same = _run(tmp_path, 4, 1000)
     print('512^3 SO4, 1000 steps: relative L2 vs oracle', {k: '%.2e' % v for k, v in errs.items()})
     assert max(errs.values()) < TOL, errs
+    assert all(same.values()), same

@@ -78,3 +78,29 @@ def test_default_mode_builds_with_nvcc(tmp_path):
     assert 'Compiled:' in r.stdout
     exe = tmp_path / 'src' / 'eigenwave3d'
     assert exe.exists(), r.stdout[-2000:]
+
+
+_NORM = re.compile(r'^(\w+)_l2: ([0-9.eE+-]+)\s*$', re.M)
+
+
+@pytest.mark.gpu
+def test_default_mode_executes_on_gpu_and_matches_oracle(tmp_path):
+    """``eigenwave3d.py default -c nvcc -x``: the generated CUDA program runs
+    the 100^3, 500-step eigenwave model on the GPU through Grid.execute and
+    prints the nine L2 errors from Grid.convergence; each equals the oracle's
+    FP64-accumulated error of the same model within 1e-4 relative (the
+    printed values carry six to seven significant digits)."""
+    script = edited_script(tmp_path)
+    env = dict(os.environ, PYTHONPATH=PKG + os.pathsep + ROOT + os.pathsep + os.environ.get('PYTHONPATH', ''))
+    r = subprocess.run([sys.executable, str(script), 'default', '-c', 'nvcc', '-x'], cwd=str(tmp_path), env=env,
+                       capture_output=True, text=True, timeout=1200)
+    assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-3000:]
+    got = {k: float(v) for k, v in _NORM.findall(r.stdout)}
+    assert len(got) == 9, r.stdout[-2000:]
+    from opesci.models import eigenwave_grid
+    from oracle import run as orun
+    g = eigenwave_grid(grid_size=(100, 100, 100), dt=0.002, ntsteps=500, space_order=4)
+    (tmp_path / 'oracle').mkdir()
+    ref = orun.run(g, str(tmp_path / 'oracle'), dump=False)['l2_fp64']
+    for k, v in ref.items():
+        assert abs(got[k] - v) <= 1e-4 * abs(v), (k, got[k], v)
