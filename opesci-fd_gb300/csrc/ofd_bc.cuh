@@ -689,7 +689,7 @@ __global__ void __launch_bounds__(256) velocity_bc_group_kernel(const GroupBc<S>
 // (BcArgs::rc set), as stress_recompute_kernel: grid-stride over virtual
 // 32 x 4 blocks (member ranges from rbegin, each member's grid rbx x rby x 12).
 template <int R, typename S>
-__global__ void __launch_bounds__(128) stress_recompute_group_kernel(const GroupBc<S> *__restrict__ tab, int n,
+__global__ void __launch_bounds__(128, 12) stress_recompute_group_kernel(const GroupBc<S> *__restrict__ tab, int n,
                                                                      int total) {
   if constexpr (R == 2 && sizeof(S) <= 4) {
     for (int vb = blockIdx.x; vb < total; vb += gridDim.x) {

@@ -1,9 +1,11 @@
 """Autotuner of the device runtime's launch knobs (the reference searched Pluto
 tile sizes with a pybench sweep, tests/pluto_tile_test.py:9-54).
 
-Knobs (ofd_set_tuning, ofd_set_persistent): per-sweep kernel (0 TMA-tiled,
-1 plain), the x chunking multiplier (CTA waves), the plain kernel's block
-shape, and persistent stepping (whole steps in one cooperative launch).  Each
+Knobs (ofd_set_tuning, ofd_set_persistent, ofd_set_ghost_schedule):
+per-sweep kernel (0 TMA-tiled, 1 plain), the x chunking multiplier (CTA
+waves), the plain kernel's block shape, persistent stepping (whole steps in
+one cooperative launch) and, for the generated space-order-4 ghosts, where
+their recompute runs (beside the stress sweep or after it) and its grid.  Each
 candidate runs a few profiled steps on a scratch handle of the same shape
 (zero fields, constant media: the kernels' cost does not depend on values),
 the fastest is kept, and results are cached in a JSON file keyed by grid
@@ -19,6 +21,9 @@ from . import runtime
 _lock = threading.Lock()
 DEFAULT = {'stress_variant': 0, 'velocity_variant': 0, 'chunk_waves': 1, 'plain_bx': 32, 'plain_by': 8,
            'persistent': 0}
+# recompute schedules tried when the configuration has generated ghosts:
+# (mode, blocks per SM); the library's default comes first
+RC_CANDIDATES = ((1, 4), (1, 2), (0, 8))
 
 
 def cache_path():
@@ -76,6 +81,7 @@ def tune(cfg, ks, kv, het=1, steps=20, use_cache=True):
     try:
         sim.set_coefficients(het, ks, kv)
         sim.set_media_const(1e-3, 1.0, 1.0)
+        gen = het and sim.set_het_ghost_coefficients()
         results = []
         best = dict(DEFAULT)
         best_t = None
@@ -105,6 +111,13 @@ def tune(cfg, ks, kv, het=1, steps=20, use_cache=True):
         results.append((k, t))
         if t < best_t:
             best, best_t = k, t
+        if gen and not best['persistent']:
+            for mode, bps in RC_CANDIDATES[1:]:
+                k = dict(best, rc_mode=mode, rc_bps=bps)
+                t = _time(sim, k, steps)
+                results.append((k, t))
+                if t < best_t:
+                    best, best_t = k, t
     finally:
         sim.close()
     if use_cache:

@@ -178,9 +178,11 @@ def run_grouped(shots, budget_bytes=150e9, keep=None, built=None, chunk_planes=0
 
     Host setup (allocation, coefficient and media uploads, one shot at a
     time in admission order) runs on a worker thread while the shots set up
-    so far step: a shot joins at the next rebuild, and while setup is still
+    so far step: a shot joins at the next rebuild.  While setup is still
     running no group advances more than ``join_steps`` steps between
-    rebuilds."""
+    rebuilds and at most two rounds are in flight (the stepping thread waits
+    for the older one, which also leaves the interpreter to the setup
+    thread)."""
     built = built if built is not None else [s.build() for s in shots]
     _last_prepare_s[0] = 0.0
     t0 = time.perf_counter()
@@ -214,6 +216,7 @@ def run_grouped(shots, budget_bytes=150e9, keep=None, built=None, chunk_planes=0
         worker = threading.Thread(target=setup, daemon=True)
         worker.start()
         sims, rem, retired = {}, {}, []
+        prev = []   # groups of the previous round, while shots are still being set up
         setting_up = True
         try:
             while True:
@@ -241,6 +244,7 @@ def run_grouped(shots, budget_bytes=150e9, keep=None, built=None, chunk_planes=0
                 by_so = {}
                 for i in live_all:
                     by_so.setdefault((shots[i].so, (shots[i].steps - rem[i]) % 2), []).append(i)
+                this_round = []
                 for key, live in by_so.items():
                     k = min(rem[i] for i in live)
                     if setting_up:
@@ -248,8 +252,16 @@ def run_grouped(shots, budget_bytes=150e9, keep=None, built=None, chunk_planes=0
                     for g in runtime.make_groups([sims[i] for i in live], chunk_planes=chunk_planes):
                         g.step(k)
                         retired.append(g)
+                        this_round.append(g)
                     for i in live:
                         rem[i] -= k
+                if setting_up:
+                    # at most two rounds in flight while shots are being set
+                    # up, so that new shots join soon; the wait also hands the
+                    # interpreter to the setup thread
+                    for g in prev:
+                        g.sync()
+                    prev = this_round
         finally:
             worker.join()
             for g in retired:

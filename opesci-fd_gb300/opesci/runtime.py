@@ -404,10 +404,14 @@ class Simulation(object):
         _check(self.lib.ofd_set_ghost_schedule(self.h, int(mode), int(blocks_per_sm)), 'ofd_set_ghost_schedule')
 
     def set_tuning(self, stress_variant=0, velocity_variant=0, chunk_waves=1, plain_bx=32, plain_by=8,
-                   persistent=0):
+                   persistent=0, rc_mode=None, rc_bps=None):
+        """Apply autotuner knobs (opesci.autotune); rc_mode / rc_bps, when
+        given, set the generated ghosts' recompute schedule."""
         _check(self.lib.ofd_set_tuning(self.h, int(stress_variant), int(velocity_variant), int(chunk_waves),
                                        int(plain_bx), int(plain_by)), 'ofd_set_tuning')
         self.set_persistent(bool(persistent))
+        if rc_mode is not None:
+            self.set_ghost_schedule(rc_mode, 4 if rc_bps is None else rc_bps)
 
     def step_profiled(self, n):
         """Advance n steps with CUDA events on the handle's stream; returns
