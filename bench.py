@@ -512,16 +512,14 @@ def main():
         dist.barrier()
     sim.sync()
     # timed region: K steps on the launch path, CUDA events on the handle's
-    # stream around all of them
-    total_ms, launches = sim.step_timed(args.steps)
+    # stream around each kernel class of every step (the roofline's kernel
+    # times) and from the first to the last (the value)
+    total_ms, cls_ms, launches = sim.step_profiled(args.steps)
     sim.sync()
     if dist is not None:
         dist.barrier()
     clocks = sampler.stop()
-    # per-kernel-class times for the roofline: a profiled pass right after,
-    # with events around each class
-    prof_steps = max(1, min(args.steps, 50))
-    _, cls_ms, _ = sim.step_profiled(prof_steps)
+    prof_steps = args.steps
     from opesci import replicas
     lups_rank = float(n) ** 3 * args.steps
     rate, secs = replicas.aggregate_rate(lups_rank, total_ms / 1e3, dist, device='cuda')
@@ -546,7 +544,25 @@ def main():
                 'step': {'bytes_per_lup': sb + vb,
                          'achieved': float(n) ** 3 * (sb + vb) * args.steps / (ms / 1e3) / 1e9},
                 'class_ms_per_step': [c / prof_steps for c in cls_ms],
-                'classes_from': 'profiled pass of %d steps after the timed region' % prof_steps}
+                'classes_from': 'the timed region: CUDA events around each kernel class of each of its %d steps'
+                                % prof_steps}
+
+    if so == 4:
+        # the stress sweep alone: at space order 4 the generated ghosts'
+        # FP64 recompute runs beside it in the step (its FP64 work shares
+        # the SM with the sweep); a short profiled pass with the recompute
+        # moved after the sweep shows the kernel by itself
+        k = min(args.steps, 20)
+        sim.set_ghost_schedule(0, 8)
+        _, cls2, _ = sim.step_profiled(k)
+        sim.set_ghost_schedule(1, 4)   # back to the library's default schedule
+        alone = cls2[0] / k
+        roofline['stress_sweep_alone'] = {
+            'avg_launch_ms': alone, 'achieved': stress_bytes / (alone / 1e3) / 1e9,
+            'frac': stress_bytes / (alone / 1e3) / 1e9 / peak,
+            'recompute_after_sweep_ms': cls2[1] / k,
+            'note': 'profiled pass of %d steps after the timed region with the ghost recompute after the '
+                    'sweep (ofd_set_ghost_schedule(0, 8)); class 1 then holds the recompute' % k}
 
     e2e = None
     if not args.no_e2e:

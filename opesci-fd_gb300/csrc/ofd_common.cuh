@@ -166,41 +166,4 @@ template <typename S> struct BcArgs {
   long rcs;
 };
 
-// Exact float -> double conversion built from the bits with integer
-// operations (sign, exponent rebiased by 1023 - 127, mantissa shifted by 29),
-// so that it takes no slot of the FP64 unit; zeros too, and the rare
-// subnormal, infinite and NaN inputs take the hardware conversion.  The
-// result equals (double)f for every input.
-__device__ __forceinline__ double f2d_exact(float f) {
-  const unsigned b = __float_as_uint(f);
-  const unsigned e = (b >> 23) & 0xffu;
-  const unsigned long long sgn = (unsigned long long)(b >> 31) << 63;
-  if (e - 1u < 254u)
-    return __longlong_as_double((long long)(sgn | ((unsigned long long)(e + 896u) << 52) |
-                                            ((unsigned long long)(b & 0x7fffffu) << 29)));
-  if ((b & 0x7fffffffu) == 0) return __longlong_as_double((long long)sgn);
-  return (double)f;
-}
-
-// The double-typed part of a generated ghost sum.  In the reference's C a
-// term holding pow(m, 2) is double and turns the rest of the sum double;
-// every float operand then meets the double one through an implicit
-// conversion.  G64 performs exactly those double operations, in the same
-// order, with the conversions done by f2d_exact; the final (float) of the
-// sum is the hardware rounding.
-struct G64 {
-  double v;
-  __device__ __forceinline__ explicit G64(double x) : v(x) {}
-  __device__ __forceinline__ explicit operator float() const { return (float)v; }
-};
-__device__ __forceinline__ G64 operator*(float a, G64 b) { return G64(f2d_exact(a) * b.v); }
-__device__ __forceinline__ G64 operator*(G64 a, float b) { return G64(a.v * f2d_exact(b)); }
-__device__ __forceinline__ G64 operator/(G64 a, float b) { return G64(a.v / f2d_exact(b)); }
-__device__ __forceinline__ G64 operator+(float a, G64 b) { return G64(f2d_exact(a) + b.v); }
-__device__ __forceinline__ G64 operator-(float a, G64 b) { return G64(f2d_exact(a) - b.v); }
-__device__ __forceinline__ G64 operator+(G64 a, float b) { return G64(a.v + f2d_exact(b)); }
-__device__ __forceinline__ G64 operator-(G64 a, float b) { return G64(a.v - f2d_exact(b)); }
-__device__ __forceinline__ G64 operator+(G64 a, G64 b) { return G64(a.v + b.v); }
-__device__ __forceinline__ G64 operator-(G64 a, G64 b) { return G64(a.v - b.v); }
-
 }  // namespace ofd

@@ -27,8 +27,6 @@ import argparse
 import json
 import math
 import os
-import queue
-import threading
 import time
 
 import numpy as np
@@ -167,22 +165,14 @@ def run_batched(shots, budget_bytes=150e9, keep=None, built=None, slice_steps=64
 _last_prepare_s = [0.0]   # host setup time of the last run_grouped call (handles, media, sources)
 
 
-def run_grouped(shots, budget_bytes=150e9, keep=None, built=None, chunk_planes=0, join_steps=64):
+def run_grouped(shots, budget_bytes=150e9, keep=None, built=None, chunk_planes=0):
     """All shots resident (admitted in order while their footprint fits the
     budget) and advanced in groups: one group per space order, every phase
     of a step one launch over all of the group's shots (ofd_group), the
     time loop a replayed two-step graph.  A group runs until its next shot
     finishes, then is rebuilt without the finished shots; groups of the two
     space orders run on their own streams at the same time.  Retired groups
-    are freed at the end, so rebuilding never waits for the device.
-
-    Host setup (allocation, coefficient and media uploads, one shot at a
-    time in admission order) runs on a worker thread while the shots set up
-    so far step: a shot joins at the next rebuild.  While setup is still
-    running no group advances more than ``join_steps`` steps between
-    rebuilds and at most two rounds are in flight (the stepping thread waits
-    for the older one, which also leaves the interpreter to the setup
-    thread)."""
+    are freed at the end, so rebuilding never waits for the device."""
     built = built if built is not None else [s.build() for s in shots]
     _last_prepare_s[0] = 0.0
     t0 = time.perf_counter()
@@ -198,80 +188,29 @@ def run_grouped(shots, budget_bytes=150e9, keep=None, built=None, chunk_planes=0
             pending.pop(0)
             group.append((i, s))
             used += fp
-        ready = queue.Queue()
-        failed = []
-
-        def setup(group=group, ready=ready, failed=failed):
-            try:
-                for i, s in group:
-                    tp = time.perf_counter()
-                    sim = prepare(s, tuned=False, built=built[i])
-                    _last_prepare_s[0] += time.perf_counter() - tp
-                    ready.put((i, sim))
-            except BaseException as e:   # reported by the stepping thread
-                failed.append(e)
-            finally:
-                ready.put(None)
-
-        worker = threading.Thread(target=setup, daemon=True)
-        worker.start()
-        sims, rem, retired = {}, {}, []
-        prev = []   # groups of the previous round, while shots are still being set up
-        setting_up = True
-        try:
-            while True:
-                wait = setting_up and not any(v > 0 for v in rem.values())
-                while setting_up:
-                    try:
-                        item = ready.get(block=wait)
-                    except queue.Empty:
-                        break
-                    wait = False
-                    if item is None:
-                        setting_up = False
-                    else:
-                        sims[item[0]] = item[1]
-                        rem[item[0]] = shots[item[0]].steps
-                if failed:
-                    raise failed[0]
-                live_all = [i for i in rem if rem[i] > 0]
-                if not live_all:
-                    if not setting_up:
-                        break
+        tp = time.perf_counter()
+        sims = {i: prepare(s, tuned=False, built=built[i]) for i, s in group}
+        _last_prepare_s[0] += time.perf_counter() - tp
+        rem = {i: s.steps for i, s in group}
+        retired = []
+        by_so = {}
+        for i, s in group:
+            by_so.setdefault(s.so, []).append(i)
+        while any(rem.values()):
+            for so, ids in by_so.items():
+                live = [i for i in ids if rem[i] > 0]
+                if not live:
                     continue
-                # members of a group stand at one time level: key by space
-                # order and the parity of the steps done
-                by_so = {}
-                for i in live_all:
-                    by_so.setdefault((shots[i].so, (shots[i].steps - rem[i]) % 2), []).append(i)
-                this_round = []
-                for key, live in by_so.items():
-                    k = min(rem[i] for i in live)
-                    if setting_up:
-                        k = min(k, join_steps)
-                    for g in runtime.make_groups([sims[i] for i in live], chunk_planes=chunk_planes):
-                        g.step(k)
-                        retired.append(g)
-                        this_round.append(g)
-                    for i in live:
-                        rem[i] -= k
-                if setting_up:
-                    # at most two rounds in flight while shots are being set
-                    # up, so that new shots join soon; the wait also hands the
-                    # interpreter to the setup thread
-                    for g in prev:
-                        g.sync()
-                    prev = this_round
-        finally:
-            worker.join()
-            for g in retired:
-                g.sync()
-            for g in retired:
-                g.close()
-            while not ready.empty():
-                item = ready.get()
-                if item is not None:
-                    sims[item[0]] = item[1]
+                k = min(rem[i] for i in live)
+                for g in runtime.make_groups([sims[i] for i in live], chunk_planes=chunk_planes):
+                    g.step(k)
+                    retired.append(g)
+                for i in live:
+                    rem[i] -= k
+        for g in retired:
+            g.sync()
+        for g in retired:
+            g.close()
         for i, s in group:
             sims[i].sync()
             if keep is not None and i in keep:

@@ -425,9 +425,8 @@ def generate_ghost_header(outdir, sigs):
              '// A(F, level, ox, oy, oz) is the field at level t0 (0) or t1 (1) at an offset',
              '// from the ghost row\'s point on the boundary plane, A.m(M, ox, oy, oz) a medium.',
              '#pragma once', '#include "ofd_common.cuh"', '', 'namespace ofd {', '',
-             '// the exact double square of a float (pow(float, 2) of the reference\'s C++),',
-             '// as a G64: the double-typed part of a sum (ofd_common.cuh)',
-             '__device__ __forceinline__ G64 ofd_pow2(float v) { return G64(f2d_exact(v) * f2d_exact(v)); }', '',
+             '// the exact double square of a float (pow(float, 2) of the reference\'s C++)',
+             '__device__ __forceinline__ double ofd_pow2(float v) { return (double)v * (double)v; }', '',
              'template <int HET> struct GenGhost4 { static constexpr bool ok = false; };', '']
     for het in (0, 1):
         g = _ghost_variant_grid(het)
