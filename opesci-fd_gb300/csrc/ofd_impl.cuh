@@ -107,10 +107,30 @@ struct Backend {
   virtual bool kmap_ok(const DevState &s, bool stress) const = 0;
 };
 
-Backend *make_backend_f32(int R);
-Backend *make_backend_f64(int R);
-Backend *make_backend_f16(int R);
-Backend *make_backend_bf16(int R);
+// One backend per (storage, radius), each defined in its own translation unit:
+// ofd_inst_<storage>.cu compiled once per radius with -DOFD_INST_R=1..4, so
+// the heavy kernel instantiations build in parallel.
+template <typename S, int R> Backend *make_backend();
+#define OFD_DECLARE_BACKENDS(S)                  \
+  template <> Backend *make_backend<S, 1>();     \
+  template <> Backend *make_backend<S, 2>();     \
+  template <> Backend *make_backend<S, 3>();     \
+  template <> Backend *make_backend<S, 4>();
+OFD_DECLARE_BACKENDS(float)
+OFD_DECLARE_BACKENDS(double)
+OFD_DECLARE_BACKENDS(__half)
+OFD_DECLARE_BACKENDS(__nv_bfloat16)
+
+template <typename S>
+inline Backend *backend_for(int R) {
+  switch (R) {
+    case 1: return make_backend<S, 1>();
+    case 2: return make_backend<S, 2>();
+    case 3: return make_backend<S, 3>();
+    case 4: return make_backend<S, 4>();
+  }
+  return nullptr;
+}
 
 // SMs of the current device (cached per device)
 inline int sm_count() {
@@ -793,15 +813,8 @@ struct Impl : Backend {
   }
 };
 
-template <typename S>
-Backend *make_backend_t(int R) {
-  switch (R) {
-    case 1: return new Impl<1, S>();
-    case 2: return new Impl<2, S>();
-    case 3: return new Impl<3, S>();
-    case 4: return new Impl<4, S>();
-  }
-  return nullptr;
-}
+// Defines make_backend<S, OFD_INST_R> in an ofd_inst_<storage>.cu unit.
+#define OFD_DEFINE_BACKEND(S) \
+  template <> Backend *make_backend<S, OFD_INST_R>() { return new Impl<OFD_INST_R, S>(); }
 
 }  // namespace ofd

@@ -1,5 +1,9 @@
-// Instantiates the (radius 1..4) kernels for __nv_bfloat16 field storage.
+// The kernels of one radius (OFD_INST_R, 1..4) for __nv_bfloat16 field storage; the
+// build compiles this unit once per radius.
 #include "ofd_impl.cuh"
+#ifndef OFD_INST_R
+#error "compile with -DOFD_INST_R=1, 2, 3 or 4"
+#endif
 namespace ofd {
-Backend *make_backend_bf16(int R) { return make_backend_t<__nv_bfloat16>(R); }
+OFD_DEFINE_BACKEND(__nv_bfloat16)
 }  // namespace ofd

@@ -426,10 +426,10 @@ int ofd_create(const ofd_config *cfg, ofd_handle **out) {
   h->s.het = 0;
   h->s.nks = h->s.nkv = 0;
   switch (cfg->storage) {
-    case OFD_F32: h->be = make_backend_f32(h->s.R); break;
-    case OFD_F64: h->be = make_backend_f64(h->s.R); break;
-    case OFD_F16: h->be = make_backend_f16(h->s.R); break;
-    case OFD_BF16: h->be = make_backend_bf16(h->s.R); break;
+    case OFD_F32: h->be = backend_for<float>(h->s.R); break;
+    case OFD_F64: h->be = backend_for<double>(h->s.R); break;
+    case OFD_F16: h->be = backend_for<__half>(h->s.R); break;
+    case OFD_BF16: h->be = backend_for<__nv_bfloat16>(h->s.R); break;
   }
   h->s.tiled.maps = nullptr;
   h->s.tiled.err = h->d_err;

@@ -35,6 +35,20 @@ def sources():
     return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith('.cu'))
 
 
+def jobs():
+    """(source, object, extra flags) per translation unit: ofd_inst_*.cu (the
+    kernels of one storage type) once per radius 1..4, the rest once."""
+    out = []
+    for src in sources():
+        base = os.path.basename(src)[:-3]
+        if base.startswith('ofd_inst_'):
+            for r in (1, 2, 3, 4):
+                out.append((src, os.path.join(LIBDIR, '%s_r%d.o' % (base, r)), ['-DOFD_INST_R=%d' % r]))
+        else:
+            out.append((src, os.path.join(LIBDIR, base + '.o'), []))
+    return out
+
+
 def _newest_input():
     paths = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if not os.path.isdir(os.path.join(CSRC, f))]
     paths += [os.path.join(CSRC, 'generated', f) for f in os.listdir(os.path.join(CSRC, 'generated'))]
@@ -53,9 +67,9 @@ def build(force=False, verbose=False, extra_flags=()):
     os.makedirs(LIBDIR, exist_ok=True)
     cc = nvcc()
 
-    def compile_one(src):
-        obj = os.path.join(LIBDIR, os.path.basename(src)[:-3] + '.o')
-        cmd = [cc] + ARCH + NVCC_FLAGS + list(extra_flags) + ['-I', INCLUDE, '-I', CSRC, '-c', src, '-o', obj]
+    def compile_one(job):
+        src, obj, defs = job
+        cmd = [cc] + ARCH + NVCC_FLAGS + list(extra_flags) + defs + ['-I', INCLUDE, '-I', CSRC, '-c', src, '-o', obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError('nvcc failed for %s:\n%s\n%s' % (src, ' '.join(cmd), r.stderr[-6000:]))
@@ -63,9 +77,9 @@ def build(force=False, verbose=False, extra_flags=()):
             print(r.stderr)
         return obj
 
-    srcs = sources()
-    with ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
-        objs = list(ex.map(compile_one, srcs))
+    js = jobs()
+    with ThreadPoolExecutor(max_workers=min(len(js), os.cpu_count() or 4)) as ex:
+        objs = list(ex.map(compile_one, js))
     tmp = LIBNAME + '.tmp'
     cmd = [cc] + ARCH + ['-shared', '-o', tmp] + objs
     r = subprocess.run(cmd, capture_output=True, text=True)
