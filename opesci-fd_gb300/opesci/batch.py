@@ -226,8 +226,10 @@ def breakdown(shots, built, budget_bytes=150e9):
     """Where the batched speed-up comes from: the shots binned by grid edge
     and space order, each bin run grouped and one by one on its own.
     Returns per bin the shot count, its share of all grid-point updates and
-    both arms' time and GLUP/s; with the bins' shares the whole workload's
-    speed-up is bounded by sum(share) / sum(share / bin speed-up)."""
+    both arms' time and GLUP/s.  Run bin by bin, the whole workload's
+    speed-up is sum(one-by-one time) / sum(grouped time); the bins holding
+    most of the work bound it: with every other bin free it could not exceed
+    sum(one-by-one time) / (those bins' grouped time)."""
     total = sum(s.lups for s in shots)
     out = []
     for so in sorted({s.so for s in shots}):

@@ -95,9 +95,9 @@ def _gpu_traces(g, media, src, wav, rec, mode):
 @pytest.mark.parametrize('so,n', [(8, 40), (4, 44)])
 def test_gpu_traces_match_oracle(so, n, tmp_path):
     """Seismograms (U, V, W, P at receivers, every step) recorded on the GPU
-    equal the oracle's: bit for bit at space order 8 (generated expressions,
-    Robertsson ghosts), within 1e-5 of each trace's peak at space order 4
-    (hand-written Levander ghosts), in every stepping path."""
+    equal the oracle's bit for bit, at space order 8 (Robertsson ghosts) and
+    at space order 4 (the generated Levander ghosts), in every stepping
+    path."""
     g, media, src, wav = _problem(tmp_path, n, so, 30, 6)
     rec = _receivers(g) + [tuple(src)]
     ref = orun.run(g, str(tmp_path), source=(src, wav), receivers=rec)['traces']
@@ -106,11 +106,8 @@ def test_gpu_traces_match_oracle(so, n, tmp_path):
         assert tr.shape == (33, 4, len(rec))
         assert not tr[30:].any()                    # rows beyond the steps run stay zero
         got = tr[:30]
-        if so == 8:
-            assert np.array_equal(got, ref), mode
-        else:
-            peak = np.maximum(np.abs(ref).max(axis=0), 1e-30)
-            assert (np.abs(got - ref).max(axis=0) / peak).max() < 1e-5, mode
+        peak = np.maximum(np.abs(ref).max(axis=0), 1e-30)
+        assert np.array_equal(got, ref), (mode, float((np.abs(got - ref).max(axis=0) / peak).max()))
     assert np.abs(ref[:, 3, -1]).max() > 0
 
 
