@@ -370,8 +370,7 @@ def run_acoustic(args, rank, world, local):
         dist.init_process_group('nccl')
     runtime.set_device(local)
     g, l1 = acoustic_problem(n, so, args.warmup + args.steps)
-    sim = runtime.RegularSimulation(runtime.regular_config_from_grid(g, variant=args.variant,
-                                                                      prefetch=args.prefetch))
+    sim = runtime.RegularSimulation(runtime.regular_config_from_grid(g, variant=args.variant))
     sim.upload(1, l1)
     sim.step(args.warmup)
     sim.sync()
@@ -459,8 +458,6 @@ def main():
     ap.add_argument('--space-order', type=int, default=4)
     ap.add_argument('--storage', default='f32')
     ap.add_argument('--variant', type=int, default=0)
-    ap.add_argument('--prefetch', type=int, default=-1,
-                    help='acoustic direct sweep: planes prefetched ahead (-1 library default, 0 none)')
     ap.add_argument('--ref-size', type=int, default=None)
     ap.add_argument('--ref-steps', type=int, default=10)
     ap.add_argument('--cpu-size', type=int, default=256)

@@ -321,8 +321,6 @@ typedef struct ofd_regular_config {
     int offset[OFD_REGULAR_MAX_TERMS][3];  /* dx, dy, dz, each in [-margin, margin] */
     double coef[OFD_REGULAR_MAX_TERMS];    /* exact value of the C literal */
     int variant;         /* 0: direct sweep (default), 1: shared-memory ring sweep */
-    int prefetch_planes; /* direct sweep: L1 prefetch of the planes this many x
-                            steps ahead (1..16); 0 none; -1 the library default */
 } ofd_regular_config;
 
 typedef struct ofd_regular ofd_regular;

@@ -53,7 +53,6 @@ constexpr int TY = 8;             // tile height along y (eight warps)
 constexpr int NT = TZ * TY;       // threads per CTA
 constexpr int MAX_MARGIN = 8;     // space order 16
 constexpr int MAXE = 8;           // ring elements per thread per plane: (32+2R)(8+2R) <= 8*256
-#define OFD_REGULAR_PREFETCH_DEFAULT 8   // planes the direct sweep prefetches ahead
 
 template <typename T>
 struct RegSweep {
@@ -63,7 +62,6 @@ struct RegSweep {
   int n1, n2, n3, m;
   int P, plane;
   int chunk;       // x planes per CTA
-  int pf;          // direct sweep: planes prefetched ahead into L1 (0: none)
   int nterms;
   signed char lvl[OFD_REGULAR_MAX_TERMS];
   signed char dx[OFD_REGULAR_MAX_TERMS];
@@ -142,17 +140,8 @@ __global__ void __launch_bounds__(NT) regular_sweep_kernel(const RegSweep<T> a) 
 // read-only path; neighbours along z and y come from the same or nearby
 // warps' lines in L1, neighbours along x from planes this thread read a few
 // iterations earlier, so memory traffic stays near the algorithmic 12 B/LUP
-// while every warp is independent.  The only lines a plane brings from DRAM
-// are the column's leading x-window value of level t (x + R) and its level
-// t-1 value; with a.pf > 0 each thread prefetches those pf planes ahead into
-// L1 (prefetch.global.L1: no registers, no waiting), after prefetching its
-// whole first window, so that many lines are in flight per warp instead of
-// the one or two its dependent loads would allow.  Every prefetched address
-// lies inside the level.
-__device__ __forceinline__ void prefetch_l1(const void *p) {
-  asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
-}
-
+// while every warp is independent (latency is hidden by occupancy, not by
+// a pipeline).
 template <typename T>
 __global__ void __launch_bounds__(NT) regular_direct_kernel(const RegSweep<T> a) {
   const int z = a.m + blockIdx.x * TZ + threadIdx.x;
@@ -164,19 +153,7 @@ __global__ void __launch_bounds__(NT) regular_direct_kernel(const RegSweep<T> a)
   const T *__restrict__ prev = a.prev;
   T *__restrict__ next = a.next;
   long g = (long)xb * a.plane + (long)y * a.P + z;
-  const int R = a.m, pf = a.pf;
-  if (pf > 0) {
-    // level t planes xb-R .. xb+R+pf-1 and level t-1 planes xb .. xb+pf-1,
-    // clipped to the array (x + R <= n1 - 1 since x < n1 - m)
-    const int hi = min(xb + R + pf, a.n1);
-    for (int x = xb - R; x < hi; ++x) prefetch_l1(cur + (long)x * a.plane + (long)y * a.P + z);
-    for (int x = xb; x < min(xb + pf, xe); ++x) prefetch_l1(prev + (long)x * a.plane + (long)y * a.P + z);
-  }
   for (int x = xb; x < xe; ++x, g += a.plane) {
-    if (pf > 0 && x + pf < xe) {
-      prefetch_l1(cur + g + (long)(pf + R) * a.plane);
-      prefetch_l1(prev + g + (long)pf * a.plane);
-    }
     T acc = T(0);
 #pragma unroll 8
     for (int k = 0; k < a.nterms; ++k) {
@@ -209,7 +186,6 @@ struct ofd_regular {
   long ti = 0;         // steps done
   int chunk = 8;
   int variant = 0;     // 0: direct, 1: shared-memory ring
-  int pf = 0;          // direct sweep: planes prefetched ahead
   dim3 grid;
   size_t smem = 0;
   RegSweep<float> a32[3];    // by ti % 3
@@ -241,7 +217,6 @@ void fill_args(ofd_regular *h, RegSweep<T> *out) {
     a.P = h->P;
     a.plane = (int)h->plane;
     a.chunk = h->chunk;
-    a.pf = h->variant == 0 ? h->pf : 0;
     a.nterms = c.nterms;
     for (int k = 0; k < c.nterms; ++k) {
       const int dx = c.offset[k][0], dy = c.offset[k][1], dz = c.offset[k][2];
@@ -264,8 +239,6 @@ int check(const ofd_regular_config *c) {
     if (c->dim[i] > (1 << 15)) return rfail(OFD_EINVAL, "dim%d = %d too large", i + 1, c->dim[i]);
   }
   if (c->variant < 0 || c->variant > 1) return rfail(OFD_EINVAL, "variant %d outside [0, 1]", c->variant);
-  if (c->prefetch_planes < -1 || c->prefetch_planes > 16)
-    return rfail(OFD_EINVAL, "prefetch_planes %d outside [-1, 16]", c->prefetch_planes);
   if (c->nterms < 1 || c->nterms > OFD_REGULAR_MAX_TERMS)
     return rfail(OFD_EINVAL, "nterms %d outside [1, %d]", c->nterms, OFD_REGULAR_MAX_TERMS);
   for (int k = 0; k < c->nterms; ++k) {
@@ -340,12 +313,10 @@ int ofd_regular_create(const ofd_regular_config *cfg, ofd_regular **out) {
   const int nx = cfg->dim[0] - 2 * m, ny = cfg->dim[1] - 2 * m, nz = cfg->dim[2] - 2 * m;
   const long tiles = (long)((nz + TZ - 1) / TZ) * ((ny + TY - 1) / TY);
   h->variant = cfg->variant;
-  h->pf = cfg->prefetch_planes < 0 ? OFD_REGULAR_PREFETCH_DEFAULT : cfg->prefetch_planes;
   long chunk;
   if (h->variant == 0) {
-    // short columns: x neighbours are still in L1 when a thread reaches
-    // them; with prefetching, longer ones amortise the first window
-    chunk = h->pf > 0 ? 32 : 16;
+    // short columns: x neighbours are still in L1 when a thread reaches them
+    chunk = 16;
   } else {
     // about eight waves of 8 resident CTAs on each of the GPU's SMs
     int sms = 152;

@@ -49,8 +49,7 @@ class ofd_regular_config(ctypes.Structure):
                 ('level', ctypes.c_int * REGULAR_MAX_TERMS),
                 ('offset', (ctypes.c_int * 3) * REGULAR_MAX_TERMS),
                 ('coef', ctypes.c_double * REGULAR_MAX_TERMS),
-                ('variant', ctypes.c_int),
-                ('prefetch_planes', ctypes.c_int)]
+                ('variant', ctypes.c_int)]
 
 
 class ofd_field_view(ctypes.Structure):
@@ -553,11 +552,10 @@ class Group(object):
 
 # --------------------------------------------------------------- regular grid
 
-def regular_config(dims, margin, terms, storage='f32', variant=0, prefetch=-1):
+def regular_config(dims, margin, terms, storage='f32', variant=0):
     """ofd_regular_config from padded dims, the margin and a term table
     [(level, (dx, dy, dz), coef), ...] (level 1: t, 0: t-1); variant 0 is
-    the direct sweep, 1 the shared-memory ring sweep; prefetch: planes the
-    direct sweep prefetches ahead (-1: the library's default, 0: none)."""
+    the direct sweep, 1 the shared-memory ring sweep."""
     st = {'f32': 0, 'float': 0, 'fp32': 0, 'f64': 3, 'double': 3, 'fp64': 3}.get(storage)
     if st is None:
         raise ValueError('regular-grid storage must be f32 or f64, not %r' % storage)
@@ -575,18 +573,17 @@ def regular_config(dims, margin, terms, storage='f32', variant=0, prefetch=-1):
             cfg.offset[k][d] = int(off[d])
         cfg.coef[k] = float(coef)
     cfg.variant = int(variant)
-    cfg.prefetch_planes = int(prefetch)
     return cfg
 
 
-def regular_config_from_grid(grid, variant=0, prefetch=-1):
+def regular_config_from_grid(grid, variant=0):
     """The device configuration of a solved one-field RegularGrid."""
     from .templates.regular_tmpl import regular_terms
     if len(grid.fields) != 1:
         raise ValueError('the regular-grid device runtime advances one field')
     terms = regular_terms(grid, grid.fields[0])
     return regular_config([d.value for d in grid.dim], grid.margin.value, terms,
-                          'f64' if grid.double else 'f32', variant=variant, prefetch=prefetch)
+                          'f64' if grid.double else 'f32', variant=variant)
 
 
 class RegularSimulation(object):

@@ -242,7 +242,6 @@ class RegularCudaTemplate(object):
         A('  cfg.margin = margin;')
         A('  cfg.storage = %s;' % storage)
         A('  cfg.nterms = %d;' % len(terms))
-        A('  cfg.prefetch_planes = -1;   // the library default')
         A('  for (int k = 0; k < %d; ++k) {' % len(terms))
         A('    cfg.level[k] = term_level[k]; cfg.coef[k] = term_coef[k];')
         A('    for (int d = 0; d < 3; ++d) cfg.offset[k][d] = term_offset[k][d];')
