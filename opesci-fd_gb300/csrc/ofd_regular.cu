@@ -140,8 +140,13 @@ __global__ void __launch_bounds__(NT) regular_sweep_kernel(const RegSweep<T> a) 
 // read-only path; neighbours along z and y come from the same or nearby
 // warps' lines in L1, neighbours along x from planes this thread read a few
 // iterations earlier, so memory traffic stays near the algorithmic 12 B/LUP
-// while every warp is independent (latency is hidden by occupancy, not by
-// a pipeline).
+// while every warp is independent.  The thread advances XU planes at a time:
+// for each term it loads the XU planes' values before the XU multiply-adds,
+// so XU times as many independent loads (and DRAM misses: the leading plane
+// of level t and level t-1) are in flight per warp; each point's chain keeps
+// the table order, so results are those of one plane at a time.
+constexpr int XU = 4;
+
 template <typename T>
 __global__ void __launch_bounds__(NT) regular_direct_kernel(const RegSweep<T> a) {
   const int z = a.m + blockIdx.x * TZ + threadIdx.x;
@@ -152,8 +157,28 @@ __global__ void __launch_bounds__(NT) regular_direct_kernel(const RegSweep<T> a)
   const T *__restrict__ cur = a.cur;
   const T *__restrict__ prev = a.prev;
   T *__restrict__ next = a.next;
-  long g = (long)xb * a.plane + (long)y * a.P + z;
-  for (int x = xb; x < xe; ++x, g += a.plane) {
+  const long pl = a.plane;
+  long g = (long)xb * pl + (long)y * a.P + z;
+  int x = xb;
+  for (; x + XU <= xe; x += XU, g += XU * pl) {
+    T acc[XU];
+#pragma unroll 4
+    for (int k = 0; k < a.nterms; ++k) {
+      const T *p = (a.lvl[k] ? cur : prev) + g + a.goff[k];
+      T v[XU];
+#pragma unroll
+      for (int u = 0; u < XU; ++u) v[u] = __ldg(p + u * pl);
+      const T c = a.coef[k];
+#pragma unroll
+      for (int u = 0; u < XU; ++u) {
+        const T q = mul_rn(c, v[u]);
+        acc[u] = k ? add_rn(acc[u], q) : q;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < XU; ++u) next[g + u * pl] = acc[u];
+  }
+  for (; x < xe; ++x, g += pl) {
     T acc = T(0);
 #pragma unroll 8
     for (int k = 0; k < a.nterms; ++k) {
