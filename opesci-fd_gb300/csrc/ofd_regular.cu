@@ -145,7 +145,7 @@ __global__ void __launch_bounds__(NT) regular_sweep_kernel(const RegSweep<T> a) 
 // so XU times as many independent loads (and DRAM misses: the leading plane
 // of level t and level t-1) are in flight per warp; each point's chain keeps
 // the table order, so results are those of one plane at a time.
-constexpr int XU = 4;
+constexpr int XU = 8;
 
 template <typename T>
 __global__ void __launch_bounds__(NT) regular_direct_kernel(const RegSweep<T> a) {
