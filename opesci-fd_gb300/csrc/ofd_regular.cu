@@ -144,10 +144,11 @@ __global__ void __launch_bounds__(NT) regular_sweep_kernel(const RegSweep<T> a) 
 // for each term it loads the XU planes' values before the XU multiply-adds,
 // so XU times as many independent loads (and DRAM misses: the leading plane
 // of level t and level t-1) are in flight per warp; each point's chain keeps
-// the table order, so results are those of one plane at a time.
-constexpr int XU = 8;
-
-template <typename T>
+// the table order, so results are those of one plane at a time.  Measured
+// at 512^3 FP32: XU = 1 / 4 / 8 / 16 gave 209 / 367 / 426 / 416 GLUP/s at
+// space order 4 and 134 / 223 / 275 / 294 at space order 8; the launch
+// takes 8 for margins up to 2 and 16 above.
+template <typename T, int XU>
 __global__ void __launch_bounds__(NT) regular_direct_kernel(const RegSweep<T> a) {
   const int z = a.m + blockIdx.x * TZ + threadIdx.x;
   const int y = a.m + blockIdx.y * TY + threadIdx.y;
@@ -403,10 +404,14 @@ int ofd_regular_step(ofd_regular *h, int nsteps) {
   for (int s = 0; s < nsteps; ++s, ++h->ti) {
     const int r = (int)(h->ti % 3);
     if (h->variant == 0) {
-      if (h->es == 4)
-        regular_direct_kernel<float><<<h->grid, dim3(TZ, TY), 0, h->stream>>>(h->a32[r]);
-      else
-        regular_direct_kernel<double><<<h->grid, dim3(TZ, TY), 0, h->stream>>>(h->a64[r]);
+      const bool wide = h->cfg.margin > 2;
+      if (h->es == 4) {
+        if (wide) regular_direct_kernel<float, 16><<<h->grid, dim3(TZ, TY), 0, h->stream>>>(h->a32[r]);
+        else regular_direct_kernel<float, 8><<<h->grid, dim3(TZ, TY), 0, h->stream>>>(h->a32[r]);
+      } else {
+        if (wide) regular_direct_kernel<double, 16><<<h->grid, dim3(TZ, TY), 0, h->stream>>>(h->a64[r]);
+        else regular_direct_kernel<double, 8><<<h->grid, dim3(TZ, TY), 0, h->stream>>>(h->a64[r]);
+      }
     } else {
       if (h->es == 4)
         regular_sweep_kernel<float><<<h->grid, dim3(TZ, TY), h->smem, h->stream>>>(h->a32[r]);
