@@ -476,12 +476,9 @@ __global__ void __launch_bounds__(256) velocity_bc_merged_kernel(const __grid_co
 // of the row and column beyond them into shared memory, once, and the
 // tangential ghosts read the fresh values from there (the merged form
 // evaluates each along-d ghost three times).  Robertsson faces as there.
-// Sides [side0, side1): the two faces of a normal touch disjoint planes, so
-// the single-handle launch gives each side its own blocks.  Every thread of
-// the block calls it (it synchronises the block).
+// Every thread of the block calls it (it synchronises the block).
 template <int R, typename S>
-__device__ __forceinline__ void velocity_gen_block(const BcArgs<S> &a, int d, int i1, int i2, int side0 = 0,
-                                                   int side1 = 2) {
+__device__ __forceinline__ void velocity_gen_block(const BcArgs<S> &a, int d, int i1, int i2) {
   if constexpr (R == 2 && sizeof(S) <= 4) {
     __shared__ float tile[9][33];
     const Geom &g = a.g;
@@ -493,7 +490,7 @@ __device__ __forceinline__ void velocity_gen_block(const BcArgs<S> &a, int d, in
     const bool act = inrange(i1, i2);
     const long sd = gstride(g, d);
     const int Fd = F_U + d;
-    for (int side = side0; side < side1; ++side) {
+    for (int side = 0; side < 2; ++side) {
       const int fb = a.face[2 * d + side];   // the same for the whole block
       if (fb == 0) continue;
       if (fb == 2) {
@@ -550,16 +547,16 @@ __device__ __forceinline__ void velocity_gen_block(const BcArgs<S> &a, int d, in
   }
 }
 
-// One launch per face normal with the generated ghost expressions, blockIdx.z
-// the side; the first launch also applies the source and advances the step
-// counter, as velocity_bc_merged_kernel.
+// One launch per face normal with the generated ghost expressions; the
+// first also applies the source and advances the step counter, as
+// velocity_bc_merged_kernel.
 template <int R, typename S>
 __global__ void __launch_bounds__(256) velocity_bc_gen_kernel(const __grid_constant__ BcArgs<S> a, S *txx, S *tyy, S *tzz, long src_off,
                                                               const float *w, int nt, long *step, float s0, float s1,
                                                               float s2) {
   const int i2 = blockIdx.x * 32 + threadIdx.x, i1 = blockIdx.y * 8 + threadIdx.y;
-  velocity_gen_block<R, S>(a, a.d, i1, i2, (int)blockIdx.z, (int)blockIdx.z + 1);
-  if (step != nullptr && a.d == 0 && blockIdx.z == 0 && i1 == 0 && i2 == 0) {
+  velocity_gen_block<R, S>(a, a.d, i1, i2);
+  if (step != nullptr && a.d == 0 && i1 == 0 && i2 == 0) {
     const long st = *step;
     if (src_off >= 0 && st < nt) {
       const float v = w[st] / 3;

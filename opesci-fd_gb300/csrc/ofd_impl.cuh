@@ -385,7 +385,7 @@ struct Impl : Backend {
     for (int d = 0; d < 3; ++d) {
       a.d = d;
       if (a.gen)
-        velocity_bc_gen_kernel<R, S><<<face_grid(s.g, d, 2), dim3(32, 8), 0, st>>>(
+        velocity_bc_gen_kernel<R, S><<<face_grid(s.g, d, 1), dim3(32, 8), 0, st>>>(
             a, fp(s, F_TXX, t1), fp(s, F_TYY, t1), fp(s, F_TZZ, t1), with_source ? s.src_off : -1L, s.d_wav, s.nt,
             with_source ? s.d_step : nullptr, s.scale[F_TXX], s.scale[F_TYY], s.scale[F_TZZ]);
       else
