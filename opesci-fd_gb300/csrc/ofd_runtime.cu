@@ -54,10 +54,10 @@ int fail_msg(int code, const char *msg) { return fail(code, "%s", msg); }
 // S. A. Figueroa, "When is double rounding innocuous?", SIGNUM 1995).
 __global__ void media_point_kernel(const float *__restrict__ rho, const float *__restrict__ vp,
                                    const float *__restrict__ vs, Geom g, float *o_beta, float *o_lam, float *o_mu,
-                                   double *inv_mu) {
+                                   double *inv_mu, int x0) {
   const int z = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
-  const int x = blockIdx.z;
+  const int x = x0 + (int)blockIdx.z;
   if (z >= g.n3 || y >= g.n2) return;
   const long i = ((long)x * g.n2 + y) * g.n3 + z;
   const long o = (long)x * g.plane + (long)y * g.P + z;
@@ -71,10 +71,10 @@ __global__ void media_point_kernel(const float *__restrict__ rho, const float *_
 }
 
 __global__ void media_avg_kernel(const float *o_beta_in, const double *__restrict__ im, Geom g, float *o_mu12,
-                                 float *o_mu13, float *o_mu23, float *o_b1, float *o_b2, float *o_b3) {
+                                 float *o_mu13, float *o_mu23, float *o_b1, float *o_b2, float *o_b3, int x0) {
   const int z = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
-  const int x = blockIdx.z;
+  const int x = x0 + (int)blockIdx.z;
   if (z >= g.n3 || y >= g.n2) return;
   const int x1 = x + 1 < g.n1 ? x + 1 : x, y1 = y + 1 < g.n2 ? y + 1 : y, z1 = z + 1 < g.n3 ? z + 1 : z;
   auto D = [&](int a, int b, int c) { return ((long)a * g.n2 + b) * g.n3 + c; };
@@ -139,6 +139,7 @@ struct ofd_handle {
   DevState s;
   Backend *be = nullptr;
   cudaStream_t stream = nullptr;
+  cudaStream_t copy_stream = nullptr;   // media uploads, overlapped with their preprocessing
   int device = 0;
   void *fields_raw = nullptr;   // one allocation for all fields
   void *media_raw = nullptr;    // one allocation for all media
@@ -472,6 +473,7 @@ int ofd_destroy(ofd_handle *h) {
   if (h->fields_raw) cudaFree(h->fields_raw);
   if (h->media_raw) cudaFree(h->media_raw);
   if (h->stream) cudaStreamDestroy(h->stream);
+  if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
   delete h;
   return OFD_OK;
 }
@@ -551,23 +553,52 @@ int ofd_set_media_const(ofd_handle *h, float beta, float lambda, float mu) {
 // Queue the media preprocessing on the handle's stream: rho, vp, vs (host or
 // device memory, dense reference layout) in, the nine effective-media arrays
 // out.  The three inputs and 1/mu pass through one stream-ordered scratch
-// allocation.
+// allocation.  The inputs move in x slabs on the handle's copy stream, and
+// each slab's per-point kernel starts as soon as its copies land (an event),
+// so the upload overlaps the FP64 preprocessing; a slab's averaging kernel,
+// which reads the next plane, follows the next slab's per-point kernel.
 static int queue_media(ofd_handle *h, const float *rho, const float *vp, const float *vs, cudaMemcpyKind kind) {
   const Geom &g = h->s.g;
   const long n = (long)g.n1 * g.n2 * g.n3;
+  const long plane = (long)g.n2 * g.n3;
   float *tmp = nullptr;
   // three float inputs, then 1/mu in double (8-byte aligned: 3n floats = 12n bytes)
   OFD_CUDA(scratch_alloc((void **)&tmp, sizeof(float) * n * 3 + sizeof(double) * n + 16, h->stream));
   double *inv_mu = (double *)(((uintptr_t)(tmp + 3 * n) + 15) & ~(uintptr_t)15);
-  OFD_CUDA(cudaMemcpyAsync(tmp, rho, sizeof(float) * n, kind, h->stream));
-  OFD_CUDA(cudaMemcpyAsync(tmp + n, vp, sizeof(float) * n, kind, h->stream));
-  OFD_CUDA(cudaMemcpyAsync(tmp + 2 * n, vs, sizeof(float) * n, kind, h->stream));
-  const dim3 blk(32, 8), grd((g.n3 + 31) / 32, (g.n2 + 7) / 8, g.n1);
-  media_point_kernel<<<grd, blk, 0, h->stream>>>(tmp, tmp + n, tmp + 2 * n, g, h->s.media[M_BETA],
-                                                 h->s.media[M_LAM], h->s.media[M_MU], inv_mu);
-  media_avg_kernel<<<grd, blk, 0, h->stream>>>(h->s.media[M_BETA], inv_mu, g, h->s.media[M_MU12], h->s.media[M_MU13],
-                                               h->s.media[M_MU23], h->s.media[M_B1], h->s.media[M_B2],
-                                               h->s.media[M_B3]);
+  if (!h->copy_stream) OFD_CUDA(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+  auto order = [](cudaStream_t from, cudaStream_t to) -> cudaError_t {
+    cudaEvent_t ev;
+    cudaError_t e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventRecord(ev, from);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(to, ev, 0);
+    cudaEventDestroy(ev);   // released once it has completed
+    return e;
+  };
+  OFD_CUDA(order(h->stream, h->copy_stream));   // the scratch exists before the copies
+  const dim3 blk(32, 8);
+  const int nslab = g.n1 < 8 ? g.n1 : 8;
+  int px0 = -1, px1 = -1;
+  auto avg = [&](int x0, int x1) {
+    const dim3 grd((g.n3 + 31) / 32, (g.n2 + 7) / 8, x1 - x0);
+    media_avg_kernel<<<grd, blk, 0, h->stream>>>(h->s.media[M_BETA], inv_mu, g, h->s.media[M_MU12],
+                                                 h->s.media[M_MU13], h->s.media[M_MU23], h->s.media[M_B1],
+                                                 h->s.media[M_B2], h->s.media[M_B3], x0);
+  };
+  for (int k = 0; k < nslab; ++k) {
+    const int x0 = (int)((long)g.n1 * k / nslab), x1 = (int)((long)g.n1 * (k + 1) / nslab);
+    const long off = (long)x0 * plane, cnt = (long)(x1 - x0) * plane;
+    OFD_CUDA(cudaMemcpyAsync(tmp + off, rho + off, sizeof(float) * cnt, kind, h->copy_stream));
+    OFD_CUDA(cudaMemcpyAsync(tmp + n + off, vp + off, sizeof(float) * cnt, kind, h->copy_stream));
+    OFD_CUDA(cudaMemcpyAsync(tmp + 2 * n + off, vs + off, sizeof(float) * cnt, kind, h->copy_stream));
+    OFD_CUDA(order(h->copy_stream, h->stream));
+    const dim3 grd((g.n3 + 31) / 32, (g.n2 + 7) / 8, x1 - x0);
+    media_point_kernel<<<grd, blk, 0, h->stream>>>(tmp, tmp + n, tmp + 2 * n, g, h->s.media[M_BETA],
+                                                   h->s.media[M_LAM], h->s.media[M_MU], inv_mu, x0);
+    if (px0 >= 0) avg(px0, px1);   // its x + 1 plane (x0) is done now
+    px0 = x0;
+    px1 = x1;
+  }
+  avg(px0, px1);
   OFD_CUDA(cudaGetLastError());
   OFD_CUDA(cudaFreeAsync(tmp, h->stream));
   return OFD_OK;
