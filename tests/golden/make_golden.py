@@ -27,10 +27,22 @@ Writes
                           overflow, extremes) and what the reference's own
                           opesci_read_model_segy (src/opesciIO.cpp:419-612),
                           compiled into the same library, reads from them.
+  receivers.txt, sources_xyz.txt, sources_{x,y,z}.raw, io.json
+                          point files with edge-case lines (signs, exponents,
+                          '.5' and '6.', an incomplete exponent, letters,
+                          missing and extra values, lines of blanks, CRLF, no
+                          final newline) and raw source signals, with what the
+                          reference's opesci_read_receivers and
+                          opesci_read_souces (src/opesciIO.cpp:345-396) read
+                          from them; and the reference's
+                          opesci_calculate_lame_costants and
+                          opesci_calculate_dt (src/opesciHandy.cpp:53-89) on
+                          seeded models with planted edge values.
 Nothing at test time reads the reference; tests read only these files.
 
     python tests/golden/make_golden.py --only resample    # just resample.json
     python tests/golden/make_golden.py --only segy        # just the SEG-Y fixtures
+    python tests/golden/make_golden.py --only io          # just the point files and model helpers
 """
 import argparse
 import json
@@ -123,12 +135,88 @@ def segy_fixtures():
               open(os.path.join(HERE, 'segy.json'), 'w'))
 
 
+RECEIVERS_TXT = (
+    'x y z receivers\n'
+    '100.5 200.25 -3e2\n'
+    '  1.5\t2.5   3.5  \n'
+    '+4 .5 6.\n'
+    '7 8\n'
+    '9 abc 10\n'
+    '11 12 13 14\n'
+    '\n'
+    '   \n'
+    '1e-3 2E+2 -0.0\n'
+    '12e 5 6\n'
+    '1.5.3 x\n'
+    '3.4028235e38 1e-45 0.1\r\n'
+    '\r\n'
+    '-.25 +.75e1 8')
+SOURCES_TXT = 'sources\n10 20 30\n40.5 50.25 60.125\n'
+
+
+def io_fixtures():
+    import ctypes
+    import numpy as np
+    lib = ctypes.CDLL(os.path.join(ROOT, 'oracle', '_ref', 'libopescihandy.so'))
+    fp = ctypes.POINTER(ctypes.c_float)
+    hexs = lambda a: [format(int(v), '08x') for v in np.asarray(a, dtype=np.float32).view(np.uint32)]  # noqa: E731
+    out = {}
+    rec = os.path.join(HERE, 'receivers.txt')
+    with open(rec, 'w', newline='') as fh:
+        fh.write(RECEIVERS_TXT)
+    buf = np.zeros(300, dtype=np.float32)
+    m = lib.ref_read_receivers(rec.encode(), buf.ctypes.data_as(fp), len(buf))
+    assert 0 < m < len(buf), m
+    out['receivers'] = {'file': 'receivers.txt', 'values_hex': hexs(buf[:m])}
+    xyz = os.path.join(HERE, 'sources_xyz.txt')
+    with open(xyz, 'w', newline='') as fh:
+        fh.write(SOURCES_TXT)
+    rng = np.random.default_rng(11)
+    paths = []
+    for k, c in enumerate('xyz'):
+        pth = os.path.join(HERE, 'sources_%s.raw' % c)
+        rng.standard_normal(17 + k).astype(np.float32).tofile(pth)
+        paths.append(pth)
+    pxyz = np.zeros(64, dtype=np.float32)
+    sig = np.zeros(256, dtype=np.float32)
+    counts = (ctypes.c_int * 4)()
+    assert lib.ref_read_sources(xyz.encode(), *[q.encode() for q in paths], pxyz.ctypes.data_as(fp), len(pxyz),
+                                sig.ctypes.data_as(fp), len(sig), counts) == 0
+    out['sources'] = {'xyz': 'sources_xyz.txt', 'signals': ['sources_x.raw', 'sources_y.raw', 'sources_z.raw'],
+                      'counts': list(counts), 'xyz_hex': hexs(pxyz[:counts[0]]),
+                      'signals_hex': hexs(sig[:counts[1] + counts[2] + counts[3]])}
+    n = 512
+    vp = (1500.0 + 3000.0 * rng.random(n)).astype(np.float32)
+    vs = (vp / np.float32(1.7) * rng.random(n).astype(np.float32)).astype(np.float32)
+    rho = (1000.0 + 2000.0 * rng.random(n)).astype(np.float32)
+    vp[:6] = [0.0, 1e-30, 3.0e19, 1.0, 7.0, -2.0]
+    vs[:6] = [0.0, 1e-30, 2.0e19, 0.5, 7.0, 1.0]
+    rho[:6] = [1.0, 1e30, 1.0, 0.0, 1.0, 3.0]
+    mu = np.zeros(n, dtype=np.float32)
+    lam = np.zeros(n, dtype=np.float32)
+    lib.ref_lame_constants(vp.ctypes.data_as(fp), vs.ctypes.data_as(fp), rho.ctypes.data_as(fp), ctypes.c_long(n),
+                           mu.ctypes.data_as(fp), lam.ctypes.data_as(fp))
+    out['lame'] = {'vp_hex': hexs(vp), 'vs_hex': hexs(vs), 'rho_hex': hexs(rho), 'mu_hex': hexs(mu),
+                   'lam_hex': hexs(lam)}
+    lib.ref_calculate_dt.restype = ctypes.c_float
+    dts = []
+    for h, arr in ((10.0, vp), (12.5, vp[6:]), (1.0, np.array([-1.0, 0.0], dtype=np.float32)),
+                   (0.1, np.array([np.nan, 2.0, 3.5], dtype=np.float32))):
+        arr = np.ascontiguousarray(arr, dtype=np.float32)
+        v = lib.ref_calculate_dt(arr.ctypes.data_as(fp), ctypes.c_long(len(arr)), ctypes.c_float(h))
+        dts.append({'h': h, 'vp_hex': hexs(arr), 'dt_hex': hexs([v])[0]})
+    out['dt'] = dts
+    json.dump({'functions': 'opesci_read_receivers, opesci_read_souces (src/opesciIO.cpp:345-396); '
+                            'opesci_calculate_lame_costants, opesci_calculate_dt (src/opesciHandy.cpp:53-89)',
+               'cases': out}, open(os.path.join(HERE, 'io.json'), 'w'))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--reference', default=os.environ.get('OPESCI_REFERENCE', os.path.join(os.path.dirname(ROOT), 'reference')),
                     help='reference checkout (default: $OPESCI_REFERENCE, else "reference" beside this repository)')
     ap.add_argument('--threads', type=int, default=os.cpu_count())
-    ap.add_argument('--only', choices=['resample', 'segy'], default=None)
+    ap.add_argument('--only', choices=['resample', 'segy', 'io'], default=None)
     args = ap.parse_args()
 
     subprocess.check_call(['make', '-C', os.path.join(ROOT, 'oracle'),
@@ -137,6 +225,8 @@ def main():
         resample_fixtures()
     if args.only in (None, 'segy'):
         segy_fixtures()
+    if args.only in (None, 'io'):
+        io_fixtures()
     if args.only is not None:
         return
     env = dict(os.environ, OMP_NUM_THREADS=str(args.threads))

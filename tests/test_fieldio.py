@@ -1,9 +1,58 @@
-"""Raw field files (the reference's dump/read format) and checkpoints that
-resume a device-resident run bit for bit."""
+"""Raw field files (the reference's dump/read format), checkpoints that
+resume a device-resident run bit for bit, source and receiver files and the
+reference's model helpers (against what the reference's own compiled
+functions gave on the fixtures in tests/golden, io.json)."""
+import json
+import os
+
 import numpy as np
 import pytest
 
 from opesci import batch, fieldio, runtime
+
+GOLDEN = os.path.join(os.path.dirname(__file__), 'golden')
+
+
+def _io():
+    with open(os.path.join(GOLDEN, 'io.json')) as fh:
+        return json.load(fh)['cases']
+
+
+def _f32(hexes):
+    return np.array([int(h, 16) for h in hexes], dtype=np.uint32).view(np.float32)
+
+
+def test_receivers_file_as_the_reference_reads_it():
+    """opesci_read_receivers on edge-case lines: signs, exponents, '.5' and
+    '6.', an incomplete exponent, letters, missing and extra values, lines
+    of blanks, CRLF, an overflowing and a subnormal value, no final
+    newline."""
+    c = _io()['receivers']
+    got = fieldio.read_receivers(os.path.join(GOLDEN, c['file']))
+    want = _f32(c['values_hex']).reshape(-1, 3)
+    assert got.shape == want.shape
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def test_sources_files_as_the_reference_reads_them():
+    c = _io()['sources']
+    xyz, sx, sy, sz = fieldio.read_sources(*[os.path.join(GOLDEN, f) for f in [c['xyz']] + c['signals']])
+    assert [xyz.size, sx.size, sy.size, sz.size] == c['counts']
+    assert np.array_equal(xyz.ravel().view(np.uint32), _f32(c['xyz_hex']).view(np.uint32))
+    assert np.array_equal(np.concatenate([sx, sy, sz]).view(np.uint32), _f32(c['signals_hex']).view(np.uint32))
+
+
+def test_lame_constants_bit_identical_to_the_reference():
+    c = _io()['lame']
+    mu, lam = fieldio.lame_constants(_f32(c['vp_hex']), _f32(c['vs_hex']), _f32(c['rho_hex']))
+    assert np.array_equal(mu.view(np.uint32), _f32(c['mu_hex']).view(np.uint32))
+    assert np.array_equal(lam.view(np.uint32), _f32(c['lam_hex']).view(np.uint32))
+
+
+def test_calculate_dt_bit_identical_to_the_reference():
+    for c in _io()['dt']:
+        got = fieldio.calculate_dt(_f32(c['vp_hex']), c['h'])
+        assert np.float32(got).view(np.uint32) == _f32([c['dt_hex']]).view(np.uint32)[0], c['h']
 
 
 def test_raw_round_trip(tmp_path):
