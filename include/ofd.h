@@ -140,9 +140,14 @@ int ofd_upload_field_device(ofd_handle *h, int field, int level, const float *de
 int ofd_download_field_device(ofd_handle *h, int field, int level, float *dev);
 int ofd_zero_fields(ofd_handle *h);
 
-/* Point source: after every step, T_ii[src] -= wavelet[step]/3 for the three
- * normal stresses while step < nt (tests/src/test_ref_iso_elastic.cpp:274-290).
- * (sx, sy, sz) is an array index including margins. */
+/* Point source: after every step, Txx[src] -= wx[step]/3, Tyy[src] -=
+ * wy[step]/3 and Tzz[src] -= wz[step]/3 while step < nt: the reference driver's
+ * x, y and z source signals (tests/src/test_ref_iso_elastic.cpp:100-126,274-290).
+ * (sx, sy, sz) is an array index including margins; nt <= 0 or a null signal
+ * removes the source.  The signals are copied; the call waits for the copy. */
+int ofd_set_source_xyz(ofd_handle *h, int sx, int sy, int sz, const float *wx, const float *wy, const float *wz,
+                       int nt);
+/* The same with one signal for all three normal stresses. */
 int ofd_set_source(ofd_handle *h, int sx, int sy, int sz, const float *wavelet, int nt);
 
 /* Receivers (seismograms; the reference records them in its hand-written

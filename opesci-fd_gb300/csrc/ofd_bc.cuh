@@ -460,10 +460,10 @@ __global__ void __launch_bounds__(256) velocity_bc_merged_kernel(const __grid_co
   if (step != nullptr && a.d == 0 && i1 == 0 && i2 == 0) {
     const long st = *step;
     if (src_off >= 0 && st < nt) {
-      const float v = w[st] / 3;
-      txx[src_off] = Storage<S>::store(Storage<S>::load(txx[src_off], 1.f / s0) - v, s0);
-      tyy[src_off] = Storage<S>::store(Storage<S>::load(tyy[src_off], 1.f / s1) - v, s1);
-      tzz[src_off] = Storage<S>::store(Storage<S>::load(tzz[src_off], 1.f / s2) - v, s2);
+      // w holds the x, y and z source signals, nt values each
+      txx[src_off] = Storage<S>::store(Storage<S>::load(txx[src_off], 1.f / s0) - w[st] / 3, s0);
+      tyy[src_off] = Storage<S>::store(Storage<S>::load(tyy[src_off], 1.f / s1) - w[nt + st] / 3, s1);
+      tzz[src_off] = Storage<S>::store(Storage<S>::load(tzz[src_off], 1.f / s2) - w[2 * nt + st] / 3, s2);
     }
     *step = st + 1;
   }
@@ -559,10 +559,10 @@ __global__ void __launch_bounds__(256) velocity_bc_gen_kernel(const __grid_const
   if (step != nullptr && a.d == 0 && i1 == 0 && i2 == 0) {
     const long st = *step;
     if (src_off >= 0 && st < nt) {
-      const float v = w[st] / 3;
-      txx[src_off] = Storage<S>::store(Storage<S>::load(txx[src_off], 1.f / s0) - v, s0);
-      tyy[src_off] = Storage<S>::store(Storage<S>::load(tyy[src_off], 1.f / s1) - v, s1);
-      tzz[src_off] = Storage<S>::store(Storage<S>::load(tzz[src_off], 1.f / s2) - v, s2);
+      // w holds the x, y and z source signals, nt values each
+      txx[src_off] = Storage<S>::store(Storage<S>::load(txx[src_off], 1.f / s0) - w[st] / 3, s0);
+      tyy[src_off] = Storage<S>::store(Storage<S>::load(tyy[src_off], 1.f / s1) - w[nt + st] / 3, s1);
+      tzz[src_off] = Storage<S>::store(Storage<S>::load(tzz[src_off], 1.f / s2) - w[2 * nt + st] / 3, s2);
     }
     *step = st + 1;
   }
@@ -675,11 +675,10 @@ __global__ void __launch_bounds__(256) velocity_bc_group_kernel(const GroupBc<S>
   if (d == 0 && local == 0 && threadIdx.x == 0 && threadIdx.y == 0 && e.step != nullptr) {
     const long st = *e.step;
     if (e.src_off >= 0 && st < e.nt) {
-      const float v = e.w[st] / 3;
       const long o = e.src_off;
-      e.txx[o] = Storage<S>::store(Storage<S>::load(e.txx[o], 1.f / e.s0) - v, e.s0);
-      e.tyy[o] = Storage<S>::store(Storage<S>::load(e.tyy[o], 1.f / e.s1) - v, e.s1);
-      e.tzz[o] = Storage<S>::store(Storage<S>::load(e.tzz[o], 1.f / e.s2) - v, e.s2);
+      e.txx[o] = Storage<S>::store(Storage<S>::load(e.txx[o], 1.f / e.s0) - e.w[st] / 3, e.s0);
+      e.tyy[o] = Storage<S>::store(Storage<S>::load(e.tyy[o], 1.f / e.s1) - e.w[e.nt + st] / 3, e.s1);
+      e.tzz[o] = Storage<S>::store(Storage<S>::load(e.tzz[o], 1.f / e.s2) - e.w[2 * e.nt + st] / 3, e.s2);
     }
     *e.step = st + 1;
   }

@@ -173,10 +173,10 @@ __global__ void __launch_bounds__(256) persistent_steps_kernel(const __grid_cons
       if (d == 0 && gtid == 0) {
         const long st = *(volatile long *)a.d_step;
         if (a.src_off >= 0 && st < a.nt) {
-          const float v = a.wav[st] / 3;
           S *t[3] = {a.st[p].out[F_TXX], a.st[p].out[F_TYY], a.st[p].out[F_TZZ]};
 #pragma unroll
           for (int q = 0; q < 3; ++q) {
+            const float v = a.wav[(long)q * a.nt + st] / 3;   // x, y, z signals
             const C old = Storage<S>::load(__ldcg(&t[q][a.src_off]), 1.f / a.ssc[q]);
             t[q][a.src_off] = Storage<S>::store(old - v, a.ssc[q]);
           }

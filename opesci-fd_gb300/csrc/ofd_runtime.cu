@@ -720,10 +720,11 @@ int ofd_zero_fields(ofd_handle *h) {
   return OFD_OK;
 }
 
-int ofd_set_source(ofd_handle *h, int sx, int sy, int sz, const float *wavelet, int nt) {
+int ofd_set_source_xyz(ofd_handle *h, int sx, int sy, int sz, const float *wx, const float *wy, const float *wz,
+                       int nt) {
   if (!h) return fail(OFD_EINVAL, "null handle");
   const Geom &g = h->s.g;
-  if (nt <= 0 || !wavelet) {
+  if (nt <= 0 || !wx || !wy || !wz) {
     h->s.src_off = -1;
     return OFD_OK;
   }
@@ -734,15 +735,23 @@ int ofd_set_source(ofd_handle *h, int sx, int sy, int sz, const float *wavelet, 
     cudaFree(h->s.d_wav);
     h->s.d_wav = nullptr;
   }
-  OFD_CUDA(cudaMalloc((void **)&h->s.d_wav, sizeof(float) * nt));
-  // stream-ordered copy: a plain cudaMemcpy from pageable memory may return
+  // the x, y and z signals back to back, nt values each
+  OFD_CUDA(cudaMalloc((void **)&h->s.d_wav, sizeof(float) * 3 * (size_t)nt));
+  // stream-ordered copies: a plain cudaMemcpy from pageable memory may return
   // before its DMA lands and is not ordered with this non-blocking stream
-  OFD_CUDA(cudaMemcpyAsync(h->s.d_wav, wavelet, sizeof(float) * nt, cudaMemcpyHostToDevice, h->stream));
+  const float *w[3] = {wx, wy, wz};
+  for (int q = 0; q < 3; ++q)
+    OFD_CUDA(cudaMemcpyAsync(h->s.d_wav + (size_t)q * nt, w[q], sizeof(float) * nt, cudaMemcpyHostToDevice,
+                             h->stream));
   OFD_CUDA(cudaStreamSynchronize(h->stream));
   h->s.nt = nt;
   h->s.src_off = (long)sx * g.plane + (long)sy * g.P + sz;
   drop_graphs(h);
   return OFD_OK;
+}
+
+int ofd_set_source(ofd_handle *h, int sx, int sy, int sz, const float *wavelet, int nt) {
+  return ofd_set_source_xyz(h, sx, sy, sz, wavelet, wavelet, wavelet, nt);
 }
 
 int ofd_set_receivers(ofd_handle *h, int nrec, const int *ijk, int nt_cap) {

@@ -95,6 +95,7 @@ def load_library():
         'ofd_download_field_device': [h, ctypes.c_int, ctypes.c_int, ctypes.c_void_p],
         'ofd_zero_fields': [h],
         'ofd_set_source': [h, ctypes.c_int, ctypes.c_int, ctypes.c_int, fptr, ctypes.c_int],
+        'ofd_set_source_xyz': [h, ctypes.c_int, ctypes.c_int, ctypes.c_int, fptr, fptr, fptr, ctypes.c_int],
         'ofd_set_receivers': [h, ctypes.c_int, P(ctypes.c_int), ctypes.c_int],
         'ofd_get_traces': [h, fptr],
         'ofd_apply_boundary_init': [h, ctypes.c_int],
@@ -351,7 +352,17 @@ class Simulation(object):
         _check(self.lib.ofd_zero_fields(self.h), 'ofd_zero_fields')
 
     def set_source(self, pos, wavelet):
-        w = np.ascontiguousarray(wavelet, dtype=np.float32)
+        """Point source at array index ``pos``: one signal for all three normal
+        stresses, or a triple (x, y, z) of equally long signals."""
+        w = np.asarray(wavelet, dtype=np.float32)
+        if w.ndim == 2:
+            if w.shape[0] != 3:
+                raise ValueError('three source signals (x, y, z) expected, got shape %s' % (w.shape,))
+            sx, sy, sz = (np.ascontiguousarray(w[q]) for q in range(3))
+            _check(self.lib.ofd_set_source_xyz(self.h, int(pos[0]), int(pos[1]), int(pos[2]), _fptr(sx),
+                                               _fptr(sy), _fptr(sz), w.shape[1]), 'ofd_set_source_xyz')
+            return
+        w = np.ascontiguousarray(w.reshape(-1))
         _check(self.lib.ofd_set_source(self.h, int(pos[0]), int(pos[1]), int(pos[2]), _fptr(w), len(w)),
                'ofd_set_source')
 

@@ -319,8 +319,17 @@ class StaggeredGrid(RegularGrid):
         return [float(w) for w in staggered_weights(self.order[1])]
 
     def set_source(self, position, wavelet):
-        """Point source injected as T_ii[src] -= s(t)/3 into the three normal
+        """Point source injected as T_ii[src] -= s_i(t)/3 into the three normal
         stresses after each step, following the hand-written reference solver
-        (tests/src/test_ref_iso_elastic.cpp:274-290).  ``position`` is an
-        array index triple (margins included); ``wavelet`` one value per step."""
-        self.source = (tuple(int(p) for p in position), list(float(w) for w in wavelet))
+        (tests/src/test_ref_iso_elastic.cpp:100-126,274-290).  ``position`` is
+        an array index triple (margins included); ``wavelet`` one value per
+        step for all three stresses, or three such signals (x, y, z) of one
+        length."""
+        w = list(wavelet)
+        if w and hasattr(w[0], '__len__'):
+            if len(w) != 3 or len({len(s) for s in w}) != 1:
+                raise ValueError('three source signals (x, y, z) of one length expected')
+            w = tuple([float(v) for v in s] for s in w)
+        else:
+            w = [float(v) for v in w]
+        self.source = (tuple(int(p) for p in position), w)

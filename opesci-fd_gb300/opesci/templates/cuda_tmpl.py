@@ -135,8 +135,11 @@ class StaggeredCudaTemplate(object):
         A('static const int field_tstag[9] = {%s};' % ', '.join(str(x) for x in tstag))
         if g.source is not None:
             (sx, sy, sz), wav = g.source
+            sigs = list(wav) if isinstance(wav, tuple) else [wav]
             A('static const int src_pos[3] = {%d, %d, %d};' % (sx, sy, sz))
-            A('static const float src_wav[%d] = {%s};' % (len(wav), ', '.join('%sf' % repr(float(w)) for w in wav)))
+            A('static const float src_wav[%d][%d] = {%s};' % (
+                len(sigs), len(sigs[0]),
+                ', '.join('{%s}' % ', '.join('%sf' % repr(float(w)) for w in sig) for sig in sigs)))
         A('')
         A('extern "C" struct OpesciGrid { %s };' % ' '.join('real_t *%s;' % n for n in names))
         A('extern "C" struct OpesciConvergence { %s };' % ' '.join('real_t %s_l2;' % n for n in names))
@@ -228,7 +231,12 @@ class StaggeredCudaTemplate(object):
         A('  }')
         A('  OFD_TRY(ofd_apply_boundary_init(g_handle, 0));')
         if g.source is not None:
-            A('  OFD_TRY(ofd_set_source(g_handle, src_pos[0], src_pos[1], src_pos[2], src_wav, %d));' % len(g.source[1]))
+            if isinstance(g.source[1], tuple):
+                A('  OFD_TRY(ofd_set_source_xyz(g_handle, src_pos[0], src_pos[1], src_pos[2], src_wav[0], src_wav[1], '
+                  'src_wav[2], %d));' % len(g.source[1][0]))
+            else:
+                A('  OFD_TRY(ofd_set_source(g_handle, src_pos[0], src_pos[1], src_pos[2], src_wav[0], %d));'
+                  % len(g.source[1]))
         A('  OFD_TRY(ofd_sync(g_handle));')
         A('  cudaEvent_t e0, e1;')
         A('  cudaEventCreate(&e0); cudaEventCreate(&e1);')

@@ -67,8 +67,21 @@ def resample_timeseries(src, dt, sdt):
     return (out * nrm2).astype(np.float32)
 
 
+def point_indices(coords, h, margin=0):
+    """Array indices of points at physical coordinates ``coords`` ((n, 3)
+    float32 metres from the first interior point), as the reference driver
+    forms them for receivers and the source
+    (tests/src/test_ref_iso_elastic.cpp:230-232,277-279):
+    ``(int)round(coor/h)`` with coor and h floats, so the quotient is rounded
+    to float and then rounded half away from zero; plus ``margin``."""
+    q = (np.asarray(coords, dtype=np.float32).reshape(-1, 3) / np.float32(h)).astype(np.float64)
+    a = np.abs(q)
+    r = np.floor(a)
+    r = np.where(a - r >= 0.5, r + 1, r)        # a - r is exact: both are the same float
+    return (np.copysign(r, q).astype(np.int64) + margin).astype(np.int32)
+
+
 def receiver_indices(coords, h, margin):
     """Array indices (margins included) of receivers at physical coordinates
     ``coords`` ((n, 3), metres from the first interior point)."""
-    c = np.asarray(coords, dtype=np.float64).reshape(-1, 3)
-    return (np.floor(c / h + 0.5).astype(np.int64) + margin).astype(np.int32)
+    return point_indices(coords, h, margin)

@@ -17,7 +17,8 @@ arithmetic):
   * heterogeneous media are defined on the full padded grid (the reference
     averages only over the interior and then reads uninitialised memory at
     the upper interior plane and in ghost formulas);
-  * an optional point source, T_ii[t1][s] -= w[ti]/3 after each step, as in
+  * an optional point source, T_ii[t1][s] -= w_i[ti]/3 after each step with
+    one signal per normal stress (or one for all three), as in
     tests/src/test_ref_iso_elastic.cpp:274-290;
   * optional receivers: after each step (ghosts and source applied) U, V, W
     and (Txx + Tyy + Tzz)/3 of level t1 at given array indices, as the
@@ -287,6 +288,19 @@ def converge_test(grid):
     return out
 
 
+def _source_signals(source):
+    """(position, wavelet) with one signal for all three normal stresses, or
+    (position, (x, y, z)) with one signal each, as the reference driver reads
+    xsrc/ysrc/zsrc (tests/src/test_ref_iso_elastic.cpp:100-126,274-290)."""
+    pos, wav = source
+    wav = list(wav)
+    if wav and hasattr(wav[0], '__len__'):
+        if len(wav) != 3 or len({len(w) for w in wav}) != 1:
+            raise ValueError('three source signals of one length expected')
+        return tuple(pos), [list(w) for w in wav]
+    return tuple(pos), [wav, wav, wav]
+
+
 def generate(grid, legacy=False, dump_prefix=None, source=None, timer=True, receivers=None):
     """The whole program: includes, ABI structs, opesci_execute,
     opesci_convergence, opesci_free and main (regular3d_tmpl.py:7-134)."""
@@ -304,8 +318,10 @@ def generate(grid, legacy=False, dump_prefix=None, source=None, timer=True, rece
         '%s %s_l2; double %s_l2_fp64;' % (grid.real_t, n, n) for n in names))
     c.add('extern "C" struct OpesciProfiling { float g_rtime; float g_ptime; float g_mflops; double loop_seconds; };')
     if source is not None:
-        (sx, sy, sz), wav = source
-        c.add('static const float _src[%d] = {%s};' % (len(wav), ', '.join(repr(float(w)) + 'f' for w in wav)))
+        (sx, sy, sz), sigs = _source_signals(source)
+        for q, wav in enumerate(sigs):
+            c.add('static const float _src%s[%d] = {%s};' % ('xyz'[q], len(wav),
+                                                           ', '.join(repr(float(w)) + 'f' for w in wav)))
     nrec = len(receivers) if receivers is not None else 0
     if nrec:
         c.add('static float _traces[%d][4][%d];' % (grid.ntsteps.value, nrec))
@@ -325,10 +341,10 @@ def generate(grid, legacy=False, dump_prefix=None, source=None, timer=True, rece
         + velocity_loop(grid) + velocity_bc(grid)
     if source is not None:
         loop += ['#pragma omp single', '{',
-                 'if(_ti < %d){' % len(source[1]),
-                 '%s[_t1][%d][%d][%d] -= _src[_ti]/3;' % (names[3], sx, sy, sz),
-                 '%s[_t1][%d][%d][%d] -= _src[_ti]/3;' % (names[4], sx, sy, sz),
-                 '%s[_t1][%d][%d][%d] -= _src[_ti]/3;' % (names[5], sx, sy, sz), '}', '}']
+                 'if(_ti < %d){' % len(sigs[0]),
+                 '%s[_t1][%d][%d][%d] -= _srcx[_ti]/3;' % (names[3], sx, sy, sz),
+                 '%s[_t1][%d][%d][%d] -= _srcy[_ti]/3;' % (names[4], sx, sy, sz),
+                 '%s[_t1][%d][%d][%d] -= _srcz[_ti]/3;' % (names[5], sx, sy, sz), '}', '}']
     if nrec:
         loop += ['#pragma omp single', '{']
         for r, (x, y, z) in enumerate(receivers):

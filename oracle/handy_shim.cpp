@@ -7,6 +7,7 @@
 // ctypes.  Compiled together with the reference's
 // src/opesciHandy.cpp and src/opesciIO.cpp (without VTK) into
 // oracle/_ref/libopescihandy.so by oracle/Makefile.
+#include <cmath>
 #include <vector>
 
 #include "opesciHandy.h"
@@ -68,4 +69,12 @@ extern "C" void ref_lame_constants(const float *vp, const float *vs, const float
 extern "C" float ref_calculate_dt(const float *vp, long n, float h) {
   std::vector<float> a(vp, vp + n);
   return opesci_calculate_dt(a, h);
+}
+
+// The index of a point at coordinate coor as the reference driver forms it
+// for receivers and the source (tests/src/test_ref_iso_elastic.cpp:230-232,
+// 277-279): (int)round(coor/h) with float operands.  The driver is a program
+// with its own main, so its one-line formula is restated here.
+extern "C" void ref_point_indices(const float *coor, long n, float h, int *out) {
+  for (long i = 0; i < n; ++i) out[i] = (int)round(coor[i] / h);
 }

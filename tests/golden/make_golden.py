@@ -37,7 +37,9 @@ Writes
                           from them; and the reference's
                           opesci_calculate_lame_costants and
                           opesci_calculate_dt (src/opesciHandy.cpp:53-89) on
-                          seeded models with planted edge values.
+                          seeded models with planted edge values, and the
+                          driver's point index (int)round(coor/h) on
+                          coordinates at and beside half-way ties.
 Nothing at test time reads the reference; tests read only these files.
 
     python tests/golden/make_golden.py --only resample    # just resample.json
@@ -206,8 +208,23 @@ def io_fixtures():
         v = lib.ref_calculate_dt(arr.ctypes.data_as(fp), ctypes.c_long(len(arr)), ctypes.c_float(h))
         dts.append({'h': h, 'vp_hex': hexs(arr), 'dt_hex': hexs([v])[0]})
     out['dt'] = dts
+    lib.ref_point_indices.restype = None
+    idx = []
+    for h in (10.0, 12.5, 7.3, 0.1, 3.0):
+        h32 = np.float32(h)
+        k = np.arange(-3, 40, dtype=np.float32)
+        ties = ((k + np.float32(0.5)) * h32).astype(np.float32)
+        near = np.concatenate([np.nextafter(ties, np.float32(-np.inf)), ties, np.nextafter(ties, np.float32(np.inf))])
+        coor = np.concatenate([near, (k * h32).astype(np.float32), rng.uniform(-50, 500, 64).astype(np.float32),
+                               np.array([0.0, -0.0, 1e-30, 2.0e6], dtype=np.float32)]).astype(np.float32)
+        res = np.zeros(len(coor), dtype=np.int32)
+        lib.ref_point_indices(coor.ctypes.data_as(fp), ctypes.c_long(len(coor)), ctypes.c_float(h),
+                              res.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
+        idx.append({'h': h, 'coor_hex': hexs(coor), 'index': res.tolist()})
+    out['indices'] = idx
     json.dump({'functions': 'opesci_read_receivers, opesci_read_souces (src/opesciIO.cpp:345-396); '
-                            'opesci_calculate_lame_costants, opesci_calculate_dt (src/opesciHandy.cpp:53-89)',
+                            'opesci_calculate_lame_costants, opesci_calculate_dt (src/opesciHandy.cpp:53-89); '
+                            'the driver\'s (int)round(coor/h) (tests/src/test_ref_iso_elastic.cpp:230-232)',
                'cases': out}, open(os.path.join(HERE, 'io.json'), 'w'))
 
 

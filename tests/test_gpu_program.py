@@ -32,12 +32,14 @@ def test_eigenwave_program_execute_and_convergence(tmp_path):
 def test_heterogeneous_program_with_source(tmp_path):
     files = {k: str(tmp_path / (k + '.raw')) for k in ('rho', 'vp', 'vs')}
     g, media, src, wav = layered_problem(36, space_order=8, ntsteps=50, seed=4, media_files=files)
-    g.set_source(src, wav)
+    # separate x, y and z signals, as the reference driver reads them
+    sigs = ([float(v) for v in wav], [float(-0.5 * v) for v in wav], [float(v) for v in np.roll(wav, 5)])
+    g.set_source(src, sigs)
     g.execute(str(tmp_path / 'layered.cu'), compiler='nvcc')
     lvl = g.ntsteps.value % 2
     got = {f: g.field_array(f, lvl) for f in FIELDS}
     g.free()
-    ref = orun.run(g, str(tmp_path / 'oracle'), source=(src, wav))
+    ref = orun.run(g, str(tmp_path / 'oracle'), source=(src, sigs))
     for f in FIELDS:
         # space order 8: Robertsson ghosts and the generated update expressions
         # reproduce the reference program bit for bit
@@ -52,3 +54,17 @@ def test_cpu_compilers_are_rejected():
     src = g.cgen_template.generate()
     for sym in ('opesci_execute', 'opesci_convergence', 'opesci_free', 'ofd_step', 'ofd_set_coefficients'):
         assert sym in src
+
+
+def test_program_source_forms():
+    """One signal goes through ofd_set_source, three (x, y, z) through
+    ofd_set_source_xyz; three signals of unequal length are rejected."""
+    g, media, src, wav = layered_problem(16, space_order=4, ntsteps=6, seed=2)
+    g.set_source(src, wav)
+    one = g.cgen_template.generate()
+    assert 'ofd_set_source(g_handle' in one and 'ofd_set_source_xyz' not in one
+    g.set_source(src, (wav, wav * 0.5, wav))
+    three = g.cgen_template.generate()
+    assert 'ofd_set_source_xyz(g_handle' in three and 'src_wav[3][6]' in three
+    with pytest.raises(ValueError):
+        g.set_source(src, (wav, wav[:3], wav))

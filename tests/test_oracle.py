@@ -61,3 +61,25 @@ def test_heterogeneous_source_oracle_runs(tmp_path):
     out = orun.run(g, str(tmp_path), source=((12, 12, 12), w), threads=2)
     assert np.abs(out['fields']['Txx']).max() > 0
     assert all(np.isfinite(a).all() for a in out['fields'].values())
+
+
+def test_three_source_signals_in_oracle(tmp_path):
+    """Separate x, y and z signals (the reference driver's xsrc, ysrc and
+    zsrc): three copies of one signal reproduce the one-signal program bit for
+    bit, and dropping the y signal changes the result."""
+    dims = (20, 20, 20)
+    rho, vp, vs = layered_media(dims, seed=5)
+    for nm, a in (('rho', rho), ('vp', vp), ('vs', vs)):
+        a.tofile(str(tmp_path / (nm + '.raw')))
+    g = elastic_grid((190.0, 190.0, 190.0), (15, 15, 15), 1e-3, 0.012, space_order=4, read=True,
+                     rho_file=str(tmp_path / 'rho.raw'), vp_file=str(tmp_path / 'vp.raw'),
+                     vs_file=str(tmp_path / 'vs.raw'), analytic=False)
+    w = [float(v) for v in ricker(12, 1e-3, 15.0)]
+    one = orun.run(g, str(tmp_path / 'one'), source=((10, 10, 10), w), threads=2)
+    three = orun.run(g, str(tmp_path / 'three'), source=((10, 10, 10), (w, w, w)), threads=2)
+    nox = orun.run(g, str(tmp_path / 'noy'), source=((10, 10, 10), (w, [0.0] * len(w), w)), threads=2)
+    for f, a in one['fields'].items():
+        assert np.array_equal(a, three['fields'][f]), f
+    assert not np.array_equal(one['fields']['Tyy'], nox['fields']['Tyy'])
+    with pytest.raises(ValueError):
+        cpp_emitter.generate(g, source=((10, 10, 10), (w, w)))

@@ -42,6 +42,23 @@ def test_receiver_indices():
     assert idx.tolist() == [[2, 3, 4], [4, 3, 2]]
 
 
+def test_point_indices_match_reference_rounding():
+    """Point indices equal the reference driver's (int)round(coor/h) (float
+    quotient, half away from zero) on coordinates at and beside half-way
+    ties, where a double quotient or round-half-even gives other indices."""
+    gold = json.load(open(os.path.join(GOLDEN, 'io.json')))['cases']['indices']
+    for case in gold:
+        coor = np.array([int(x, 16) for x in case['coor_hex']], dtype=np.uint32).view(np.float32)
+        want = np.array(case['index'])
+        got = traces.point_indices(np.stack([coor, coor[::-1], coor], axis=1), case['h'])
+        assert np.array_equal(got[:, 0], want), case['h']
+        assert np.array_equal(got[:, 1], want[::-1]), case['h']
+        assert np.array_equal(traces.point_indices(np.stack([coor] * 3, axis=1), case['h'], margin=4)[:, 2],
+                              want + 4)
+        # the planted ties separate it from a plain double-precision rounding
+        assert (np.round(coor.astype(np.float64) / case['h']).astype(np.int64) != want).any(), case['h']
+
+
 def _receivers(g):
     m = g.order[1] // 2
     n = [d.value for d in g.dim]
