@@ -170,6 +170,16 @@ int ofd_get_traces(ofd_handle *h, float *host);
  * memory, x fastest, the reference's array order).  No handle needed. */
 int ofd_segy_decode_ibm(const void *file, long file_size, int nx, int ny, int nz, int swap_endian, float *out);
 
+/* Write name.vts: a VTK XML structured grid of one host field of
+ * dims[0] x dims[1] x dims[2] floats (last index fastest), as the reference's
+ * opesci_dump_field_vts_3d (src/opesciIO.cpp:614-667) does for the generated
+ * code's output_vts step (opesci/regulargrid.py:702-719): point coordinates
+ * (index - margin) * spacing in the reference's insertion order, one
+ * point-data array "field".  Appended raw data, UInt64 headers, no
+ * compression.  Host only; no handle or GPU needed. */
+int ofd_write_field_vts_3d(const char *name, const int dims[3], const float spacing[3], int margin,
+                           const float *field);
+
 /* Ghost cells of one level as the reference's initialise_bc does for the
  * initial level (staggeredgrid.py:866-879): stress mirrors, then velocity
  * ghosts. */

@@ -120,6 +120,7 @@ def load_library():
         'ofd_group_eligible': [h],
         'ofd_segy_decode_ibm': [ctypes.c_void_p, ctypes.c_long, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                 ctypes.c_int, fptr],
+        'ofd_write_field_vts_3d': [ctypes.c_char_p, P(ctypes.c_int), fptr, ctypes.c_int, fptr],
         'ofd_group_query': [h],
         'ofd_group_sync': [h],
         'ofd_group_destroy': [h],

@@ -120,6 +120,7 @@ class StaggeredCudaTemplate(object):
         A('#include <cstdlib>')
         A('#include <cstring>')
         A('#include <cmath>')
+        A('#include <string>')
         A('#include <vector>')
         A('#include <cuda_runtime.h>')
         A('#include "ofd.h"')
@@ -241,7 +242,24 @@ class StaggeredCudaTemplate(object):
         A('  cudaEvent_t e0, e1;')
         A('  cudaEventCreate(&e0); cudaEventCreate(&e1);')
         A('  cudaEventRecord(e0, st);')
-        A('  OFD_TRY(ofd_step(g_handle, ntsteps));')
+        if g.output_vts:
+            # the output_vts step after every time step (staggered3d_tmpl.py:56-58,
+            # regulargrid.py:702-719): U of the new level to U_<ti>.vts with the
+            # reference's margin argument of 2; its dims {dim1, dim1, dim1} are
+            # the grid's for cubic grids, which are the only ones it writes whole
+            A('  {')
+            A('    std::vector<float> vts_buf(n);')
+            A('    const int vts_dims[3] = {n1, n2, n3};')
+            A('    const float vts_spacing[3] = {dx1, dx2, dx3};')
+            A('    for (int _ti = 0; _ti < ntsteps; ++_ti) {')
+            A('      OFD_TRY(ofd_step(g_handle, 1));')
+            A('      OFD_TRY(ofd_download_field(g_handle, 0, (_ti + 1) % 2, vts_buf.data()));')
+            A('      const std::string vtkfile = "U_" + std::to_string(_ti);')
+            A('      OFD_TRY(ofd_write_field_vts_3d(vtkfile.c_str(), vts_dims, vts_spacing, 2, vts_buf.data()));')
+            A('    }')
+            A('  }')
+        else:
+            A('  OFD_TRY(ofd_step(g_handle, ntsteps));')
         A('  cudaEventRecord(e1, st);')
         A('  OFD_TRY(ofd_sync(g_handle));')
         A('  float ms = 0.f;')

@@ -68,3 +68,24 @@ def test_program_source_forms():
     assert 'ofd_set_source_xyz(g_handle' in three and 'src_wav[3][6]' in three
     with pytest.raises(ValueError):
         g.set_source(src, (wav, wav[:3], wav))
+
+
+@pytest.mark.gpu
+def test_program_output_vts(tmp_path, monkeypatch):
+    """output_vts: the program writes U of the new level to U_<ti>.vts after
+    every step (regulargrid.py:702-719); the first dump equals the oracle
+    after one step and the last equals the published final field."""
+    from opesci import vts
+    monkeypatch.chdir(tmp_path)
+    g = eigenwave_grid(grid_size=(24, 24, 24), ntsteps=4, space_order=4)
+    g.output_vts = True
+    g.execute(str(tmp_path / 'eigen_vts.cu'), compiler='nvcc')
+    last = g.field_array('U', g.ntsteps.value % 2)
+    g.free()
+    dumps = [vts.read_vts(str(tmp_path / ('U_%d.vts' % t))) for t in range(4)]
+    assert all(d['extent'] == tuple(last.shape) for d in dumps)
+    assert np.array_equal(dumps[-1]['arrays']['field'], last.reshape(-1))
+    one = eigenwave_grid(grid_size=(24, 24, 24), ntsteps=1, space_order=4)
+    ref = orun.run(one, str(tmp_path / 'oracle'))
+    first, want = dumps[0]['arrays']['field'].astype(np.float64), ref['fields']['U'].reshape(-1).astype(np.float64)
+    assert np.linalg.norm(first - want) <= 1e-5 * np.linalg.norm(want)
