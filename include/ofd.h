@@ -129,6 +129,11 @@ int ofd_set_ghost_coefficients(ofd_handle *h, int het, const float *kg, int nkg)
  * which the generated program's opesci_execute does with these calls. */
 int ofd_upload_field(ofd_handle *h, int field, int level, const float *host);
 int ofd_download_field(ofd_handle *h, int field, int level, float *host);
+/* The same for OFD_F64 storage with double host arrays, exact both ways: the
+ * reference's double switch (regulargrid.py:27-28) publishes double arrays.
+ * Other storage types report OFD_EINVAL. */
+int ofd_upload_field_f64(ofd_handle *h, int field, int level, const double *host);
+int ofd_download_field_f64(ofd_handle *h, int field, int level, double *host);
 /* The same queued on the handle's stream without waiting (no counterpart in
  * the reference): several fields' copies then run back to back, and with
  * pinned host memory they overlap other host work.  The host array must stay

@@ -714,6 +714,31 @@ int ofd_download_field_async(ofd_handle *h, int field, int level, float *host) {
   return queue_download(h, field, level, host);
 }
 
+// FP64 storage: double host arrays copied as they are, one pitched copy.
+static int transfer_f64(ofd_handle *h, int field, int level, double *host, bool up) {
+  int rc = check_fl(h, field, level);
+  if (rc) return rc;
+  if (!host) return fail(OFD_EINVAL, "null host array");
+  if (h->s.storage != OFD_F64) return fail(OFD_EINVAL, "FP64 field transfers need OFD_F64 storage");
+  const Geom &g = h->s.g;
+  double *dev = (double *)h->s.field[field] + (size_t)level * g.level;
+  const size_t row = sizeof(double) * g.n3, pitch = sizeof(double) * g.P, rows = (size_t)g.n1 * g.n2;
+  if (up)
+    OFD_CUDA(cudaMemcpy2DAsync(dev, pitch, host, row, row, rows, cudaMemcpyDefault, h->stream));
+  else
+    OFD_CUDA(cudaMemcpy2DAsync(host, row, dev, pitch, row, rows, cudaMemcpyDefault, h->stream));
+  OFD_CUDA(cudaStreamSynchronize(h->stream));
+  return OFD_OK;
+}
+
+int ofd_upload_field_f64(ofd_handle *h, int field, int level, const double *host) {
+  return transfer_f64(h, field, level, const_cast<double *>(host), true);
+}
+
+int ofd_download_field_f64(ofd_handle *h, int field, int level, double *host) {
+  return transfer_f64(h, field, level, host, false);
+}
+
 int ofd_zero_fields(ofd_handle *h) {
   if (!h) return fail(OFD_EINVAL, "null handle");
   OFD_CUDA(cudaMemsetAsync(h->fields_raw, 0, h->field_bytes * NF, h->stream));

@@ -150,11 +150,14 @@ def checkpoint(sim, directory):
     """Write both levels of the nine fields and the step count of ``sim``."""
     os.makedirs(directory, exist_ok=True)
     sim.sync()
+    dtype = np.dtype(sim.host_dtype)
     for f in runtime.FIELDS:
         for lvl in (0, 1):
-            dump_field_raw(os.path.join(directory, '%s_%d' % (f, lvl)), sim.download(f, lvl))
+            # native values of the handle's host type (float64 for FP64 storage)
+            np.ascontiguousarray(sim.download(f, lvl), dtype=dtype).tofile(
+                os.path.join(directory, '%s_%d.raw' % (f, lvl)))
     with open(os.path.join(directory, 'state.json'), 'w') as fh:
-        json.dump({'steps': sim.steps, 'dims': list(sim.dims)}, fh)
+        json.dump({'steps': sim.steps, 'dims': list(sim.dims), 'dtype': dtype.name}, fh)
 
 
 def restore(sim, directory):
@@ -165,7 +168,11 @@ def restore(sim, directory):
     if list(sim.dims) != st['dims']:
         raise ValueError('checkpoint of a %s grid, simulation is %s' % (st['dims'], list(sim.dims)))
     n = int(np.prod(sim.dims))
+    dtype = np.dtype(st.get('dtype', 'float32'))
     for f in runtime.FIELDS:
         for lvl in (0, 1):
-            sim.upload(f, lvl, read_simple_binary_ptr(os.path.join(directory, '%s_%d.raw' % (f, lvl)), n))
+            a = np.fromfile(os.path.join(directory, '%s_%d.raw' % (f, lvl)), dtype=dtype)
+            if len(a) < n:
+                raise ValueError('checkpoint field %s_%d holds %d values, %d needed' % (f, lvl, len(a), n))
+            sim.upload(f, lvl, a[:n])
     sim.steps = st['steps']

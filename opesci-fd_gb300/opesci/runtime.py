@@ -89,6 +89,8 @@ def load_library():
         'ofd_set_media_async': [h, fptr, fptr, fptr],
         'ofd_upload_field': [h, ctypes.c_int, ctypes.c_int, fptr],
         'ofd_download_field': [h, ctypes.c_int, ctypes.c_int, fptr],
+        'ofd_upload_field_f64': [h, ctypes.c_int, ctypes.c_int, P(ctypes.c_double)],
+        'ofd_download_field_f64': [h, ctypes.c_int, ctypes.c_int, P(ctypes.c_double)],
         'ofd_upload_field_async': [h, ctypes.c_int, ctypes.c_int, fptr],
         'ofd_download_field_async': [h, ctypes.c_int, ctypes.c_int, fptr],
         'ofd_upload_field_device': [h, ctypes.c_int, ctypes.c_int, ctypes.c_void_p],
@@ -316,17 +318,34 @@ class Simulation(object):
         r, p, s = self._arr(rho), self._arr(vp), self._arr(vs)
         _check(self.lib.ofd_set_media(self.h, _fptr(r), _fptr(p), _fptr(s)), 'ofd_set_media')
 
+    @property
+    def host_dtype(self):
+        """Element type of upload()/download() arrays: float64 for FP64
+        storage, else float32."""
+        return np.float64 if self.cfg.storage == STORAGE['f64'] else np.float32
+
     def upload(self, field, level, array):
         f = FIELDS.index(field) if isinstance(field, str) else field
+        if self.host_dtype == np.float64:
+            a = np.ascontiguousarray(array, dtype=np.float64).reshape(self.dims)
+            _check(self.lib.ofd_upload_field_f64(self.h, f, level, a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))),
+                   'ofd_upload_field_f64')
+            return
         a = self._arr(array)
         _check(self.lib.ofd_upload_field(self.h, f, level, _fptr(a)), 'ofd_upload_field')
 
     def download(self, field, level=None):
+        """One field level in the reference layout: float64 for FP64 storage
+        (exact), else float32."""
         f = FIELDS.index(field) if isinstance(field, str) else field
         if level is None:
             level = self.steps % 2
-        out = np.empty(self.dims, dtype=np.float32)
-        _check(self.lib.ofd_download_field(self.h, f, level, _fptr(out)), 'ofd_download_field')
+        out = np.empty(self.dims, dtype=self.host_dtype)
+        if out.dtype == np.float64:
+            _check(self.lib.ofd_download_field_f64(self.h, f, level, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))),
+                   'ofd_download_field_f64')
+        else:
+            _check(self.lib.ofd_download_field(self.h, f, level, _fptr(out)), 'ofd_download_field')
         return out
 
     def download_all_async(self, outs, level=None):

@@ -67,9 +67,18 @@ class StaggeredCudaTemplate(object):
                              'expressions of libofd' % key)
         ks, kv = tabs['stress'][1], tabs['velocity'][1]
         fmt = lambda a: ', '.join('%sf' % repr(float(x)) for x in a)  # noqa: E731
-        return ['static const float ofd_ks[%d] = {%s};' % (len(ks), fmt(ks)),
-                'static const float ofd_kv[%d] = {%s};' % (len(kv), fmt(kv)),
-                'constexpr int ofd_het = %d;' % (1 if g.read else 0)], len(ks), len(kv)
+        out = ['static const float ofd_ks[%d] = {%s};' % (len(ks), fmt(ks)),
+               'static const float ofd_kv[%d] = {%s};' % (len(kv), fmt(kv)),
+               'constexpr int ofd_het = %d;' % (1 if g.read else 0)]
+        # space order 4 with Levander faces: the printed ghost equations' literal
+        # table, when their structure is the prebuilt one (not for FP64 storage)
+        gt = None if g.double else cuda_gen.ghost_table(g)
+        if gt is not None and pre.get('ghost') == gt[0]:
+            out.append('static const float ofd_kg[%d] = {%s};' % (len(gt[1]), fmt(gt[1])))
+            self._nkg = len(gt[1])
+        else:
+            self._nkg = 0
+        return out, len(ks), len(kv)
 
     def _solutions(self):
         g = self.grid
@@ -96,9 +105,6 @@ class StaggeredCudaTemplate(object):
 
     def generate(self):
         g = self.grid
-        if g.double:
-            raise NotImplementedError('the CUDA program template publishes float fields; run FP64 models '
-                                      'through opesci.runtime with storage="f64"')
         names = [ccode(f.label) for f in g.fields]
         has_sol = [getattr(f, 'sol', None) is not None for f in g.fields]
         stag = [[1 if f.staggered[d + 1] else 0 for d in range(3)] for f in g.fields]
@@ -125,7 +131,7 @@ class StaggeredCudaTemplate(object):
         A('#include <cuda_runtime.h>')
         A('#include "ofd.h"')
         A('')
-        A('typedef float real_t;')
+        A('typedef %s real_t;' % ('double' if g.double else 'float'))
         A('#define OFD_TRY(call) do { int _r = (call); if (_r) { fprintf(stderr, "%s: %s\\n", #call, ofd_last_error()); return _r; } } while (0)')
         A('#define CU_TRY(call) do { cudaError_t _e = (call); if (_e != cudaSuccess) { fprintf(stderr, "%s: %s\\n", #call, cudaGetErrorString(_e)); return -2; } } while (0)')
         A('')
@@ -155,18 +161,18 @@ class StaggeredCudaTemplate(object):
         A('}')
         A('')
         A('// analytic value of field f at time t on its own index range, reference layout')
-        A('__global__ void init_field(float *out, int f, int s0, int s1, int s2, double t) {')
+        A('__global__ void init_field(real_t *out, int f, int s0, int s1, int s2, double t) {')
         A('  const long n = (long)n1 * n2 * n3;')
         A('  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {')
         A('    const int z = (int)(i % n3); const long r = i / n3; const int y = (int)(r % n2); const int x = (int)(r / n2);')
         A('    const bool in = x >= margin && x < n1 - margin - s0 && y >= margin && y < n2 - margin - s1 &&')
         A('                    z >= margin && z < n3 - margin - s2;')
-        A('    out[i] = in ? (float)sol_field(f, coord(dx1, x, s0), coord(dx2, y, s1), coord(dx3, z, s2), t) : 0.0f;')
+        A('    out[i] = in ? (real_t)sol_field(f, coord(dx1, x, s0), coord(dx2, y, s1), coord(dx3, z, s2), t) : (real_t)0;')
         A('  }')
         A('}')
         A('')
         A('// FP64 squared error against the analytic solution, one partial per block')
-        A('__global__ void l2_partial(const float *fld, int f, int s0, int s1, int s2, double t, double *partial) {')
+        A('__global__ void l2_partial(const real_t *fld, int f, int s0, int s1, int s2, double t, double *partial) {')
         A('  const long n = (long)n1 * n2 * n3;')
         A('  double acc = 0.0;')
         A('  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {')
@@ -200,7 +206,7 @@ class StaggeredCudaTemplate(object):
         A('  memset(&cfg, 0, sizeof(cfg));')
         A('  cfg.dim[0] = n1; cfg.dim[1] = n2; cfg.dim[2] = n3;')
         A('  cfg.space_order = %d;' % g.order[1])
-        A('  cfg.storage = OFD_F32;')
+        A('  cfg.storage = %s;' % ('OFD_F64' if g.double else 'OFD_F32'))
         A('  cfg.legacy_bc = %d;' % (1 if getattr(g, 'legacy_bc', False) else 0))
         for i, fc in enumerate(faces):
             A('  cfg.free_surface[%d] = %s;' % (i, fc))
@@ -212,6 +218,8 @@ class StaggeredCudaTemplate(object):
         A('  if (g_handle) { ofd_destroy(g_handle); g_handle = nullptr; }')
         A('  OFD_TRY(ofd_create(&cfg, &g_handle));')
         A('  OFD_TRY(ofd_set_coefficients(g_handle, ofd_het, ofd_ks, %d, ofd_kv, %d));' % (nks, nkv))
+        if self._nkg:
+            A('  OFD_TRY(ofd_set_ghost_coefficients(g_handle, ofd_het, ofd_kg, %d));' % self._nkg)
         if g.read:
             A('  {')
             A('    std::vector<float> rho_a(n), vp_a(n), vs_a(n);')
@@ -221,14 +229,23 @@ class StaggeredCudaTemplate(object):
             A('  }')
         else:
             A('  OFD_TRY(ofd_set_media_const(g_handle, beta, lambda, mu));')
-        A('  float *tmp = nullptr;')
-        A('  CU_TRY(cudaMalloc((void **)&tmp, sizeof(float) * n));')
+        A('  real_t *tmp = nullptr;')
+        A('  CU_TRY(cudaMalloc((void **)&tmp, sizeof(real_t) * n));')
         A('  cudaStream_t st = (cudaStream_t)ofd_stream(g_handle);')
+        if g.double:
+            A('  std::vector<double> init_host(n);')
         A('  for (int f = 0; f < 9; ++f) {')
         A('    if (!field_has_sol[f]) continue;')
         A('    const double t0 = field_tstag[f] ? dt / 2 : 0.0;')
         A('    init_field<<<1216, 256, 0, st>>>(tmp, f, field_stag[f][0], field_stag[f][1], field_stag[f][2], t0);')
-        A('    OFD_TRY(ofd_upload_field_device(g_handle, f, 0, tmp));')
+        if g.double:
+            # FP64 storage takes double host arrays: the initial level goes
+            # through the host once, exactly
+            A('    CU_TRY(cudaMemcpyAsync(init_host.data(), tmp, sizeof(double) * n, cudaMemcpyDeviceToHost, st));')
+            A('    CU_TRY(cudaStreamSynchronize(st));')
+            A('    OFD_TRY(ofd_upload_field_f64(g_handle, f, 0, init_host.data()));')
+        else:
+            A('    OFD_TRY(ofd_upload_field_device(g_handle, f, 0, tmp));')
         A('  }')
         A('  OFD_TRY(ofd_apply_boundary_init(g_handle, 0));')
         if g.source is not None:
@@ -271,7 +288,10 @@ class StaggeredCudaTemplate(object):
         A('    void *p = nullptr;')
         A('    if (posix_memalign(&p, 4096, sizeof(real_t) * 2 * n)) return -3;')
         A('    *dst[f] = (real_t *)p;')
-        A('    for (int l = 0; l < 2; ++l) OFD_TRY(ofd_download_field(g_handle, f, l, (float *)p + l * n));')
+        if g.double:
+            A('    for (int l = 0; l < 2; ++l) OFD_TRY(ofd_download_field_f64(g_handle, f, l, (double *)p + l * n));')
+        else:
+            A('    for (int l = 0; l < 2; ++l) OFD_TRY(ofd_download_field(g_handle, f, l, (float *)p + l * n));')
         A('  }')
         A('  cudaFree(tmp);')
         A('  return 0;')
@@ -283,8 +303,8 @@ class StaggeredCudaTemplate(object):
         A('  const long n = (long)n1 * n2 * n3;')
         A('  const int level = ntsteps % 2;')
         A('  real_t *out[9] = {%s};' % ', '.join('&conv->%s_l2' % nm for nm in names))
-        A('  float *tmp = nullptr; double *part = nullptr;')
-        A('  CU_TRY(cudaMalloc((void **)&tmp, sizeof(float) * n));')
+        A('  real_t *tmp = nullptr; double *part = nullptr;')
+        A('  CU_TRY(cudaMalloc((void **)&tmp, sizeof(real_t) * n));')
         A('  CU_TRY(cudaMalloc((void **)&part, sizeof(double) * 1024));')
         A('  cudaStream_t st = (cudaStream_t)ofd_stream(g_handle);')
         A('  std::vector<double> hp(1024);')
@@ -292,7 +312,12 @@ class StaggeredCudaTemplate(object):
         A('    *out[f] = 0;')
         A('    if (!field_has_sol[f]) continue;')
         A('    const double tn = dt * ntsteps + (field_tstag[f] ? dt / 2.0 : 0.0);')
-        A('    OFD_TRY(ofd_download_field_device(g_handle, f, level, tmp));')
+        if g.double:
+            # the published double arrays of opesci_execute, level ntsteps % 2
+            A('    real_t *pub[9] = {%s};' % ', '.join('grid->%s' % nm for nm in names))
+            A('    CU_TRY(cudaMemcpyAsync(tmp, pub[f] + (size_t)level * n, sizeof(double) * n, cudaMemcpyHostToDevice, st));')
+        else:
+            A('    OFD_TRY(ofd_download_field_device(g_handle, f, level, tmp));')
         A('    l2_partial<<<1024, 256, 0, st>>>(tmp, f, field_stag[f][0], field_stag[f][1], field_stag[f][2], tn, part);')
         A('    CU_TRY(cudaMemcpyAsync(hp.data(), part, sizeof(double) * 1024, cudaMemcpyDeviceToHost, st));')
         A('    CU_TRY(cudaStreamSynchronize(st));')

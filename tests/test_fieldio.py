@@ -2,6 +2,7 @@
 resume a device-resident run bit for bit, source and receiver files and the
 reference's model helpers (against what the reference's own compiled
 functions gave on the fixtures in tests/golden, io.json)."""
+import ctypes
 import json
 import os
 
@@ -86,3 +87,45 @@ def test_checkpoint_resumes_bit_for_bit(so, n, tmp_path):
         assert np.array_equal(ref.download(f), b.download(f)), f
     ref.close()
     b.close()
+
+
+@pytest.mark.gpu
+def test_fp64_transfers_and_checkpoint_exact(tmp_path):
+    """FP64 storage: double host arrays go in and come out unchanged, and a
+    checkpoint of an FP64 run (written as float64) resumes bit for bit."""
+    from opesci.models import layered_problem
+    g, media, src, wav = layered_problem(36, space_order=4, ntsteps=24, seed=21)
+
+    def make():
+        sim = runtime.Simulation(runtime.config_from_grid(g, storage='f64'))
+        sim.set_coefficients_from_grid(g)
+        sim.set_media(*media)
+        sim.set_source(src, wav)
+        return sim
+
+    sim = make()
+    vals = np.random.default_rng(6).standard_normal(sim.dims) * (1.0 + 2.0 ** -40)
+    sim.upload('Txz', 1, vals)
+    back = sim.download('Txz', 1)
+    assert back.dtype == np.float64 and np.array_equal(back, vals)
+    sim.zero()
+    sim.step(24)
+    sim.sync()
+    ref = {f: sim.download(f) for f in runtime.FIELDS}
+    sim.close()
+    a = make()
+    a.step(9)
+    fieldio.checkpoint(a, str(tmp_path / 'ck64'))
+    a.close()
+    b = make()
+    fieldio.restore(b, str(tmp_path / 'ck64'))
+    b.step(15)
+    b.sync()
+    for f in runtime.FIELDS:
+        assert np.array_equal(ref[f], b.download(f)), f
+    assert np.abs(ref['Txx']).max() > 0
+    b.close()
+    f32 = runtime.Simulation(runtime.config_from_grid(g))
+    rc = f32.lib.ofd_download_field_f64(f32.h, 0, 0, back.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+    assert rc == -1 and 'OFD_F64' in f32.lib.ofd_last_error().decode()
+    f32.close()

@@ -56,6 +56,20 @@ def test_cpu_compilers_are_rejected():
         assert sym in src
 
 
+def test_program_storage_and_ghost_tables():
+    """double=True emits FP64 storage and double transfers; a float SO4
+    Levander model passes its printed ghost equations' literals."""
+    g = eigenwave_grid(grid_size=(12, 12, 12), ntsteps=3, double=True)
+    src = g.cgen_template.generate()
+    for s in ('typedef double real_t;', 'cfg.storage = OFD_F64;', 'ofd_upload_field_f64', 'ofd_download_field_f64'):
+        assert s in src, s
+    assert 'ofd_set_ghost_coefficients' not in src
+    f = eigenwave_grid(grid_size=(12, 12, 12), ntsteps=3).cgen_template.generate()
+    assert 'typedef float real_t;' in f and 'OFD_F32' in f and 'ofd_set_ghost_coefficients(g_handle' in f
+    g8 = eigenwave_grid(grid_size=(12, 12, 12), ntsteps=3, space_order=8).cgen_template.generate()
+    assert 'ofd_set_ghost_coefficients' not in g8
+
+
 def test_program_source_forms():
     """One signal goes through ofd_set_source, three (x, y, z) through
     ofd_set_source_xyz; three signals of unequal length are rejected."""
@@ -89,3 +103,25 @@ def test_program_output_vts(tmp_path, monkeypatch):
     ref = orun.run(one, str(tmp_path / 'oracle'))
     first, want = dumps[0]['arrays']['field'].astype(np.float64), ref['fields']['U'].reshape(-1).astype(np.float64)
     assert np.linalg.norm(first - want) <= 1e-5 * np.linalg.norm(want)
+
+
+@pytest.mark.gpu
+def test_double_program_matches_fp64_oracle(tmp_path):
+    """The double switch (regulargrid.py:27-28): FP64 storage and
+    arithmetic, double fields published through OpesciGrid and double norms
+    through OpesciConvergence, against the oracle built with double."""
+    g = eigenwave_grid(grid_size=(24, 24, 24), ntsteps=40, space_order=4, double=True)
+    g.execute(str(tmp_path / 'eigen64.cu'), compiler='nvcc')
+    l2 = g.convergence()
+    lvl = g.ntsteps.value % 2
+    got = {f: g.field_array(f, lvl) for f in FIELDS}
+    g.free()
+    ref = orun.run(g, str(tmp_path / 'oracle'))
+    state = np.sqrt(sum(np.linalg.norm(ref['fields'][f]) ** 2 for f in FIELDS))
+    for f in FIELDS:
+        assert got[f].dtype == np.float64 and ref['fields'][f].dtype == np.float64
+        # FP64 storage evaluates the restated ghost formulas with exact
+        # constants where the printed ones carry float (F) literals: the
+        # fields differ by about 3e-9 of the state norm (measured)
+        assert np.linalg.norm(got[f] - ref['fields'][f]) <= 1e-7 * state, f
+        assert abs(l2[f + '_l2'] - ref['l2_fp64'][f]) <= 1e-5 * ref['l2_fp64'][f], f
