@@ -85,6 +85,7 @@ class Grid(object):
 
         class OpesciProfiling(Structure):
             _fields_ = [(v, c_float) for v in ('rtime', 'ptime', 'mflops')]
+            _fields_ += [(ev, ctypes.c_longlong) for ev in getattr(self, '_papi_events', [])]
 
         self._arg_grid = OpesciGrid()
         self._arg_profiling = OpesciProfiling()
@@ -96,7 +97,15 @@ class Grid(object):
         if rc != 0:
             raise RuntimeError('opesci_execute failed with status %d' % rc)
         if self.profiling:
+            # the reference's report (grid.py:122-130); the time is the GPU time
+            # loop's (CUDA events) and MFlops/s counts the update expressions'
+            # operations, PAPI counters being host-CPU events
+            for ev in getattr(self, '_papi_events', []):
+                print('PAPI:: %s: not counted on the GPU' % ev)
             print('GPU time loop: %f (sec)' % self._arg_profiling.rtime)
+            print('Max real_time: %f (sec)' % self._arg_profiling.rtime)
+            print('Max proc_time: %f (sec)' % self._arg_profiling.ptime)
+            print('Total MFlops/s: %f' % self._arg_profiling.mflops)
 
     def convergence(self):
         """L2 norms against the analytic solution (grid.py:132-156)."""

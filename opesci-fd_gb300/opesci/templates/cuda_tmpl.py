@@ -80,6 +80,12 @@ class StaggeredCudaTemplate(object):
             self._nkg = 0
         return out, len(ks), len(kv)
 
+    def _flops_per_point(self):
+        """Additions plus multiplications of the nine update expressions."""
+        g = self.grid
+        v, s = g.get_velocity_kernel_ai(), g.get_stress_kernel_ai()
+        return int(v[2] + v[3] + s[2] + s[3])
+
     def _solutions(self):
         g = self.grid
         out = []
@@ -150,7 +156,11 @@ class StaggeredCudaTemplate(object):
         A('')
         A('extern "C" struct OpesciGrid { %s };' % ' '.join('real_t *%s;' % n for n in names))
         A('extern "C" struct OpesciConvergence { %s };' % ' '.join('real_t %s_l2;' % n for n in names))
-        A('extern "C" struct OpesciProfiling { float g_rtime; float g_ptime; float g_mflops; };')
+        # PAPI event slots (regulargrid.py:350-354): kept for the struct layout
+        # the caller defines; hardware counters of the host CPU have no meaning
+        # for a GPU run and stay zero
+        papi = ''.join(' long long g_%s;' % e for e in getattr(g, '_papi_events', []))
+        A('extern "C" struct OpesciProfiling { float g_rtime; float g_ptime; float g_mflops;%s };' % papi)
         A('')
         L.extend(self._solutions())
         A('')
@@ -283,6 +293,16 @@ class StaggeredCudaTemplate(object):
         A('  cudaEventElapsedTime(&ms, e0, e1);')
         A('  cudaEventDestroy(e0); cudaEventDestroy(e1);')
         A('  profiling->g_rtime = ms / 1000.0f; profiling->g_ptime = ms / 1000.0f; profiling->g_mflops = 0.0f;')
+        for e in getattr(g, '_papi_events', []):
+            A('  profiling->g_%s = 0;' % e)
+        if g.profiling:
+            # the update expressions' additions and multiplications per interior
+            # point (get_kernel_ai's counts, regulargrid.py:293-327) over the timed loop
+            fl = self._flops_per_point()
+            A('  {')
+            A('    const double pts = (double)(n1 - 2 * margin) * (n2 - 2 * margin) * (n3 - 2 * margin);')
+            A('    if (ms > 0.f) profiling->g_mflops = (float)(%d.0 * pts * ntsteps / (ms / 1000.0) / 1e6);' % fl)
+            A('  }')
         A('  real_t **dst[9] = {%s};' % ', '.join('&grid->%s' % nm for nm in names))
         A('  for (int f = 0; f < 9; ++f) {')
         A('    void *p = nullptr;')

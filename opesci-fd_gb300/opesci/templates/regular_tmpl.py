@@ -180,7 +180,8 @@ class RegularCudaTemplate(object):
         A('')
         A('extern "C" struct OpesciGrid { real_t *%s; };' % name)
         A('extern "C" struct OpesciConvergence { real_t %s_l2; };' % name)
-        A('extern "C" struct OpesciProfiling { float g_rtime; float g_ptime; float g_mflops; };')
+        papi = ''.join(' long long g_%s;' % e for e in getattr(g, '_papi_events', []))
+        A('extern "C" struct OpesciProfiling { float g_rtime; float g_ptime; float g_mflops;%s };' % papi)
         A('')
         A('typedef real_t (*levels_t)[n1][n2][n3];')
         A('')
@@ -266,6 +267,16 @@ class RegularCudaTemplate(object):
         A('  cudaEventElapsedTime(&ms, e0, e1);')
         A('  cudaEventDestroy(e0); cudaEventDestroy(e1);')
         A('  profiling->g_rtime = ms / 1000.0f; profiling->g_ptime = ms / 1000.0f; profiling->g_mflops = 0.0f;')
+        for e in getattr(g, '_papi_events', []):
+            A('  profiling->g_%s = 0;' % e)
+        if g.profiling:
+            # one multiplication per term and one addition per term after the
+            # first, per interior point, over the timed loop
+            A('  {')
+            A('    const double pts = (double)(n1 - 2 * margin) * (n2 - 2 * margin) * (n3 - 2 * margin);')
+            A('    if (ms > 0.f) profiling->g_mflops = (float)(%d.0 * pts * ntsteps / (ms / 1000.0) / 1e6);'
+              % (2 * len(terms) - 1))
+            A('  }')
         A('  void *p = nullptr;')
         A('  if (posix_memalign(&p, 4096, sizeof(real_t) * 3 * n)) return -3;')
         A('  grid->%s = (real_t *)p;' % name)

@@ -70,6 +70,20 @@ def test_program_storage_and_ghost_tables():
     assert 'ofd_set_ghost_coefficients' not in g8
 
 
+def test_program_profiling_fields():
+    """profiling: MFlops/s from the update expressions' operation counts
+    (get_kernel_ai); PAPI event slots keep the caller's struct layout."""
+    g = eigenwave_grid(grid_size=(12, 12, 12), ntsteps=3)
+    assert 'g_mflops = (float)(' not in g.cgen_template.generate()
+    g.profiling = True
+    g.set_papi_events(['PAPI_L1_DCM', 'PAPI_TOT_INS'])
+    src = g.cgen_template.generate()
+    v, s = g.get_velocity_kernel_ai(), g.get_stress_kernel_ai()
+    assert 'g_mflops = (float)(%d.0 * pts' % (v[2] + v[3] + s[2] + s[3]) in src
+    assert 'float g_mflops; long long g_PAPI_L1_DCM; long long g_PAPI_TOT_INS; };' in src
+    assert 'profiling->g_PAPI_TOT_INS = 0;' in src
+
+
 def test_program_source_forms():
     """One signal goes through ofd_set_source, three (x, y, z) through
     ofd_set_source_xyz; three signals of unequal length are rejected."""
