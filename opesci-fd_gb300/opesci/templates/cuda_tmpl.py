@@ -64,7 +64,8 @@ class StaggeredCudaTemplate(object):
         pre = cuda_gen.prebuilt_signatures().get(key)
         if pre is None or pre['stress'] != tabs['stress'][0] or pre['velocity'] != tabs['velocity'][0]:
             raise ValueError('the update expressions of this model (%s) do not match the prebuilt CUDA '
-                             'expressions of libofd' % key)
+                             'expressions of libofd: the device kernels are built for the velocity-stress '
+                             'equations with the expand and eval_const switches on (their defaults)' % key)
         ks, kv = tabs['stress'][1], tabs['velocity'][1]
         fmt = lambda a: ', '.join('%sf' % repr(float(x)) for x in a)  # noqa: E731
         out = ['static const float ofd_ks[%d] = {%s};' % (len(ks), fmt(ks)),

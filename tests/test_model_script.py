@@ -71,13 +71,19 @@ def test_print_edit_is_the_only_change(tmp_path):
 def test_default_mode_builds_with_nvcc(tmp_path):
     script = edited_script(tmp_path)
     env = dict(os.environ, PYTHONPATH=PKG + os.pathsep + os.environ.get('PYTHONPATH', ''))
-    r = subprocess.run([sys.executable, str(script), 'default', '-c', 'nvcc'], cwd=str(tmp_path), env=env,
+    # the script's own switches: VTS output, profiling with PAPI event slots
+    # and Pluto tiling (a no-op for the CUDA target)
+    r = subprocess.run([sys.executable, str(script), 'default', '-c', 'nvcc', '-o', '-p', '--papi-events',
+                        'PAPI_TOT_CYC', '--pluto', '--tile', '4 4 32'], cwd=str(tmp_path), env=env,
                        capture_output=True, text=True, timeout=900)
     assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-3000:]
     assert 'require dt < ' in r.stdout
     assert 'Compiled:' in r.stdout
     exe = tmp_path / 'src' / 'eigenwave3d'
     assert exe.exists(), r.stdout[-2000:]
+    src = (tmp_path / 'src' / 'eigenwave3d.cpp').read_text()
+    for s in ('ofd_write_field_vts_3d(', 'long long g_PAPI_TOT_CYC;', 'profiling->g_mflops = (float)('):
+        assert s in src, s
 
 
 _NORM = re.compile(r'^(\w+)_l2: ([0-9.eE+-]+)\s*$', re.M)
