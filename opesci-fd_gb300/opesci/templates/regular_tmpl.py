@@ -148,7 +148,7 @@ class RegularCudaTemplate(object):
         A = L.append
         A('// Generated by opesci (RegularCudaTemplate): regular-grid scheme, order %s,' % (g.order,))
         A('// grid %s, %d steps.' % ([d.value for d in g.dim], g.ntsteps.value))
-        for inc in ('cstdio', 'cstdlib', 'cstring', 'cmath', 'vector', 'cuda_runtime.h'):
+        for inc in ('cstdio', 'cstdlib', 'cstring', 'cmath', 'string', 'vector', 'cuda_runtime.h'):
             A('#include <%s>' % inc)
         A('#include "ofd.h"')
         A('')
@@ -260,7 +260,26 @@ class RegularCudaTemplate(object):
         A('  cudaEvent_t e0, e1;')
         A('  cudaEventCreate(&e0); cudaEventCreate(&e1);')
         A('  cudaEventRecord(e0, st);')
-        A('  OFD_TRY(ofd_regular_step(g_handle, ntsteps));')
+        if g.output_vts:
+            # the output_vts step after every time step (regulargrid.py:702-719):
+            # the new level _t2 = (_ti + 2) % 3 to <field>_<ti>.vts with the
+            # reference's margin argument of 2, as float values
+            sp = [s.name for s in g.spacing]
+            A('  {')
+            A('    std::vector<real_t> vts_raw(n);')
+            A('    std::vector<float> vts_buf(n);')
+            A('    const int vts_dims[3] = {n1, n2, n3};')
+            A('    const float vts_spacing[3] = {(float)%s, (float)%s, (float)%s};' % tuple(sp))
+            A('    for (int _ti = 0; _ti < ntsteps; ++_ti) {')
+            A('      OFD_TRY(ofd_regular_step(g_handle, 1));')
+            A('      OFD_TRY(ofd_regular_download(g_handle, (_ti + 2) % 3, vts_raw.data()));')
+            A('      for (long i = 0; i < n; ++i) vts_buf[i] = (float)vts_raw[i];')
+            A('      const std::string vtkfile = "%s_" + std::to_string(_ti);' % name)
+            A('      OFD_TRY(ofd_write_field_vts_3d(vtkfile.c_str(), vts_dims, vts_spacing, 2, vts_buf.data()));')
+            A('    }')
+            A('  }')
+        else:
+            A('  OFD_TRY(ofd_regular_step(g_handle, ntsteps));')
         A('  cudaEventRecord(e1, st);')
         A('  OFD_TRY(ofd_regular_sync(g_handle));')
         A('  float ms = 0.f;')

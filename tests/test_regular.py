@@ -114,7 +114,12 @@ def test_generated_program_compiles(tmp_path):
     lib = build.build()
     for double in (False, True):
         g = simplewave_grid(grid_size=(16, 16, 16), space_order=4, ntsteps=3, double=double)
+        # with the output_vts and profiling switches: the per-step VTS dump
+        # and the MFlops/s figure are compiled in as well
+        g.output_vts = double
+        g.profiling = double
         src = g.cgen_template.generate()
+        assert ('ofd_write_field_vts_3d(' in src) == double and ('g_mflops = (float)(' in src) == double
         for sym in ('opesci_execute', 'opesci_convergence', 'opesci_free', 'ofd_regular_create', 'ofd_regular_step'):
             assert sym in src
         cu = tmp_path / ('simplewave_%d.cu' % double)
@@ -175,6 +180,25 @@ def test_reference_default_case_program(tmp_path):
         assert np.array_equal(got[lvl], ref['levels']['MAIN_GRID'][lvl]), lvl
     want = ref['l2_fp64']['MAIN_GRID']
     assert abs(l2['MAIN_GRID_l2'] - want) <= 1e-5 * want
+
+
+@pytest.mark.gpu
+def test_program_output_vts(tmp_path, monkeypatch):
+    """output_vts: the new level after every step in MAIN_GRID_<ti>.vts
+    (regulargrid.py:702-719); the last dump is the published level
+    (ntsteps + 1) % 3."""
+    from opesci import vts
+    monkeypatch.chdir(tmp_path)
+    g = simplewave_grid(grid_size=(20, 20, 20), dt=0.002, space_order=4, ntsteps=4)
+    g.output_vts = True
+    g.execute(str(tmp_path / 'simplewave_vts.cu'), compiler='nvcc')
+    got = g.field_array('MAIN_GRID')
+    g.free()
+    ref = orun.run_regular(g, str(tmp_path / 'oracle'))['levels']['MAIN_GRID']
+    last = vts.read_vts(str(tmp_path / 'MAIN_GRID_3.vts'))
+    assert np.array_equal(last['arrays']['field'], got[5 % 3].reshape(-1))
+    assert np.array_equal(last['arrays']['field'], ref[5 % 3].reshape(-1))
+    assert all((tmp_path / ('MAIN_GRID_%d.vts' % t)).exists() for t in range(4))
 
 
 def test_device_config_validation_without_gpu():
