@@ -107,7 +107,12 @@ def test_program_output_vts(tmp_path, monkeypatch):
     monkeypatch.chdir(tmp_path)
     g = eigenwave_grid(grid_size=(24, 24, 24), ntsteps=4, space_order=4)
     g.output_vts = True
+    g.profiling = True
+    g.set_papi_events(['PAPI_TOT_CYC'])
     g.execute(str(tmp_path / 'eigen_vts.cu'), compiler='nvcc')
+    # profiling: the time loop's CUDA-event time and MFlops/s, PAPI slot zero
+    assert g._arg_profiling.rtime > 0 and g._arg_profiling.mflops > 0
+    assert g._arg_profiling.PAPI_TOT_CYC == 0
     last = g.field_array('U', g.ntsteps.value % 2)
     g.free()
     dumps = [vts.read_vts(str(tmp_path / ('U_%d.vts' % t))) for t in range(4)]
