@@ -53,6 +53,27 @@ def test_footprint_and_validation_without_gpu(lib):
     assert 'too small' in lib.ofd_last_error().decode()
 
 
+def test_null_arguments_rejected_without_gpu(lib):
+    """Entry points added for FP64 transfers, three-signal sources and VTS
+    output report OFD_EINVAL for null handles and arrays before touching the
+    device."""
+    import numpy as np
+    d = np.zeros(8)
+    dp = d.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    assert lib.ofd_upload_field_f64(None, 0, 0, dp) == -1
+    assert lib.ofd_download_field_f64(None, 0, 0, dp) == -1
+    f = np.zeros(8, dtype=np.float32)
+    fp = f.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    assert lib.ofd_set_source_xyz(None, 1, 1, 1, fp, fp, fp, 8) == -1
+    assert 'null handle' in lib.ofd_last_error().decode()
+    dims = (ctypes.c_int * 3)(2, 2, 2)
+    sp = (ctypes.c_float * 3)(1.0, 1.0, 1.0)
+    assert lib.ofd_write_field_vts_3d(b'x', dims, sp, 0, None) == -1
+    bad = (ctypes.c_int * 3)(2, 0, 2)
+    assert lib.ofd_write_field_vts_3d(b'x', bad, sp, 0, fp) == -1
+    assert 'positive' in lib.ofd_last_error().decode()
+
+
 def test_python_binding_covers_every_entry_point(lib):
     """opesci/runtime.py (the ctypes stub of the integration guide) gives
     every function of include/ofd.h an argument signature."""
