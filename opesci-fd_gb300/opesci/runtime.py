@@ -265,7 +265,9 @@ class Simulation(object):
         """Literal tables of the grid's generated update expressions, after
         checking that their structure is the prebuilt one."""
         from .templates import cuda_gen
-        tabs = cuda_gen.sweep_tables(grid)
+        # with the expand or eval_const switch off, the same update in the
+        # default printed form (cuda_gen.default_form)
+        tabs, _ = cuda_gen.model_tables(grid)
         key = 'so%d_%s' % (grid.order[1], 'het' if grid.read else 'const')
         pre = cuda_gen.prebuilt_signatures().get(key)
         if pre is None or pre['stress'] != tabs['stress'][0] or pre['velocity'] != tabs['velocity'][0]:
@@ -301,7 +303,7 @@ class Simulation(object):
         from .templates import cuda_gen
         if self.cfg.storage == STORAGE['f64']:
             return False
-        tab = cuda_gen.ghost_table(grid)
+        tab = cuda_gen.model_ghost_table(grid)
         if tab is None:
             return False
         key = 'so4_%s' % ('het' if grid.read else 'const')
@@ -609,10 +611,10 @@ def regular_config(dims, margin, terms, storage='f32', variant=0):
 
 def regular_config_from_grid(grid, variant=0):
     """The device configuration of a solved one-field RegularGrid."""
-    from .templates.regular_tmpl import regular_terms
+    from .templates.regular_tmpl import model_terms
     if len(grid.fields) != 1:
         raise ValueError('the regular-grid device runtime advances one field')
-    terms = regular_terms(grid, grid.fields[0])
+    terms = model_terms(grid, grid.fields[0])
     return regular_config([d.value for d in grid.dim], grid.margin.value, terms,
                           'f64' if grid.double else 'f32', variant=variant)
 

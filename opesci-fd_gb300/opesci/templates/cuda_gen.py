@@ -21,6 +21,7 @@ csrc/generated/sweeps_gen.cuh, ghosts_gen.cuh (the space-order-4 Levander
 ghost expressions) and signatures.json for space orders 2-8 with constant and
 heterogeneous media.
 """
+import contextlib
 import hashlib
 import json
 import math
@@ -95,6 +96,44 @@ def kernel_text(grid, fields):
 def signature(exprs):
     canon = '\n'.join(re.sub(r'K\[\d+\]', 'K', e) for e in exprs)
     return hashlib.sha1(canon.encode()).hexdigest()[:16]
+
+
+@contextlib.contextmanager
+def default_form(grid):
+    """The grid's update and ghost expressions printed with the expand and
+    eval_const switches on (their defaults), whatever the grid's own
+    switches.  The device kernels are built for that printed form; with the
+    switches off the reference prints the same update unexpanded or with
+    named constants, which rounds differently (by ~1e-7 relative)."""
+    saved = (grid.expand, grid.eval_const)
+    grid.expand, grid.eval_const = True, True
+    try:
+        yield grid
+    finally:
+        grid.expand, grid.eval_const = saved
+
+
+def model_tables(grid):
+    """sweep_tables of the grid in its own printed form when the prebuilt
+    kernels evaluate it, else in the default form: (tables, own_form)."""
+    key = 'so%d_%s' % (grid.order[1], 'het' if grid.read else 'const')
+    pre = prebuilt_signatures().get(key)
+    tabs = sweep_tables(grid)
+    if pre is not None and pre['stress'] == tabs['stress'][0] and pre['velocity'] == tabs['velocity'][0]:
+        return tabs, True
+    if grid.expand and grid.eval_const:
+        return tabs, True
+    with default_form(grid):
+        return sweep_tables(grid), False
+
+
+def model_ghost_table(grid):
+    """ghost_table of the grid, in the default printed form when its expand
+    or eval_const switch is off."""
+    if grid.expand and grid.eval_const:
+        return ghost_table(grid)
+    with default_form(grid):
+        return ghost_table(grid)
 
 
 def sweep_tables(grid):

@@ -59,13 +59,15 @@ class StaggeredCudaTemplate(object):
     def _tables(self):
         from . import cuda_gen
         g = self.grid
-        tabs = cuda_gen.sweep_tables(g)
+        # with the expand or eval_const switch off, the same update in the
+        # default printed form (cuda_gen.default_form)
+        tabs, _ = cuda_gen.model_tables(g)
         key = 'so%d_%s' % (g.order[1], 'het' if g.read else 'const')
         pre = cuda_gen.prebuilt_signatures().get(key)
         if pre is None or pre['stress'] != tabs['stress'][0] or pre['velocity'] != tabs['velocity'][0]:
             raise ValueError('the update expressions of this model (%s) do not match the prebuilt CUDA '
                              'expressions of libofd: the device kernels are built for the velocity-stress '
-                             'equations with the expand and eval_const switches on (their defaults)' % key)
+                             'equations' % key)
         ks, kv = tabs['stress'][1], tabs['velocity'][1]
         fmt = lambda a: ', '.join('%sf' % repr(float(x)) for x in a)  # noqa: E731
         out = ['static const float ofd_ks[%d] = {%s};' % (len(ks), fmt(ks)),
@@ -73,7 +75,7 @@ class StaggeredCudaTemplate(object):
                'constexpr int ofd_het = %d;' % (1 if g.read else 0)]
         # space order 4 with Levander faces: the printed ghost equations' literal
         # table, when their structure is the prebuilt one (not for FP64 storage)
-        gt = None if g.double else cuda_gen.ghost_table(g)
+        gt = None if g.double else cuda_gen.model_ghost_table(g)
         if gt is not None and pre.get('ghost') == gt[0]:
             out.append('static const float ofd_kg[%d] = {%s};' % (len(gt[1]), fmt(gt[1])))
             self._nkg = len(gt[1])

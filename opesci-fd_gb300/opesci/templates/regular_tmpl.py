@@ -34,7 +34,7 @@ import numpy as np
 from ..codeprinter import ccode
 from .cuda_gen import decimal_to_f32
 
-__all__ = ['RegularCudaTemplate', 'regular_terms', 'split_terms']
+__all__ = ['RegularCudaTemplate', 'model_terms', 'regular_terms', 'split_terms']
 
 _COEF_FLOAT = re.compile(r'^(\d+\.\d*(?:e[+-]?\d+)?)F$')
 _COEF_INT = re.compile(r'^(\d+)$')
@@ -79,6 +79,18 @@ def _coef_value(text):
     if m:
         return np.float32(np.float32(int(m.group(1))) / np.float32(int(m.group(2))))
     raise ValueError('coefficient %r is not a literal' % text)
+
+
+def model_terms(grid, field):
+    """regular_terms of the grid's update; with the expand or eval_const
+    switch off, of the same update in the default printed form
+    (cuda_gen.default_form), which rounds differently from the reference's
+    unexpanded or named-constant C by ~1e-7 relative."""
+    if grid.expand and grid.eval_const:
+        return regular_terms(grid, field)
+    from .cuda_gen import default_form
+    with default_form(grid):
+        return regular_terms(grid, field)
 
 
 def regular_terms(grid, field):
@@ -136,7 +148,7 @@ class RegularCudaTemplate(object):
         name = ccode(f.label)
         real = g.real_t
         storage = 'OFD_F64' if g.double else 'OFD_F32'
-        terms = regular_terms(g, f)
+        terms = model_terms(g, f)
         init1 = ccode(g.initial_kernel(f))
         init2 = ccode(g.second_initial_kernel(f))
         sol = getattr(f, 'sol', None)

@@ -352,3 +352,18 @@ def test_three_source_signals_match_oracle(tmp_path, so):
     # the y and z signals are not the x one: a one-signal run differs
     one = run_problem_gpu(g, media, src, wav)
     assert not np.array_equal(one['Tyy'], runs['steps']['Tyy'])
+
+
+@pytest.mark.parametrize('switches', [dict(eval_const=False), dict(expand=False, eval_const=False)])
+def test_switches_off_match_oracle(tmp_path, switches):
+    """expand/eval_const off: the device runs the default printed form of
+    the same update; the oracle prints the grid's own form (named constants
+    evaluated at run time), which rounds differently.  Each field within
+    1e-5 of the state norm (oracle against oracle the two forms differ by
+    ~3e-7)."""
+    g = eigenwave_grid(grid_size=(32, 32, 32), ntsteps=60, space_order=4, **switches)
+    got = run_eigen_gpu(g)
+    ref = orun.run(g, str(tmp_path))
+    errs = rel_errors(got, ref['fields'], state_norm=True)
+    assert max(errs.values()) < TOL, errs
+    assert all(getattr(g, k) is False for k in switches)

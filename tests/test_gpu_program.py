@@ -84,6 +84,22 @@ def test_program_profiling_fields():
     assert 'profiling->g_PAPI_TOT_INS = 0;' in src
 
 
+def test_switches_off_use_the_default_form():
+    """expand=False or eval_const=False: the program runs the same update in
+    the default printed form (the prebuilt kernels' form), with the printed
+    ghost table of that form; the grid keeps its switches."""
+    from opesci.templates import cuda_gen
+    base = cuda_gen.sweep_tables(eigenwave_grid(grid_size=(12, 12, 12), ntsteps=3))
+    for kw in (dict(expand=False), dict(eval_const=False), dict(expand=False, eval_const=False)):
+        g = eigenwave_grid(grid_size=(12, 12, 12), ntsteps=3, **kw)
+        tabs, own = cuda_gen.model_tables(g)
+        assert not own and all(g.__dict__[k] is False for k in kw)
+        for kind in ('stress', 'velocity'):
+            assert tabs[kind][0] == base[kind][0] and np.array_equal(tabs[kind][1], base[kind][1])
+        src = g.cgen_template.generate()
+        assert 'ofd_set_ghost_coefficients(g_handle' in src
+
+
 def test_program_source_forms():
     """One signal goes through ofd_set_source, three (x, y, z) through
     ofd_set_source_xyz; three signals of unequal length are rejected."""

@@ -96,6 +96,20 @@ def test_term_table_rejects_unexpanded_kernels():
         regular_terms(g, g.fields[0])
 
 
+def test_switches_off_use_the_default_form():
+    """With expand or eval_const off the device runs the same update in the
+    default printed form; the grid's switches are left as they were."""
+    from opesci.templates.regular_tmpl import model_terms
+    ref = regular_terms(simplewave_grid(grid_size=(10, 10, 10), space_order=4, ntsteps=2),
+                        simplewave_grid(grid_size=(10, 10, 10), space_order=4, ntsteps=2).fields[0])
+    for sw in ('expand', 'eval_const'):
+        g = simplewave_grid(grid_size=(10, 10, 10), space_order=4, ntsteps=2)
+        setattr(g, sw, False)
+        assert model_terms(g, g.fields[0]) == ref
+        assert getattr(g, sw) is False
+        assert 'ofd_regular_create' in g.cgen_template.generate()
+
+
 def test_oracle_second_initialisation(tmp_path):
     """The reference's second initialisation with v = 1 on a zero level 0
     gives level 1 = v*dt on the interior, zero on the margins."""
@@ -180,6 +194,27 @@ def test_reference_default_case_program(tmp_path):
         assert np.array_equal(got[lvl], ref['levels']['MAIN_GRID'][lvl]), lvl
     want = ref['l2_fp64']['MAIN_GRID']
     assert abs(l2['MAIN_GRID_l2'] - want) <= 1e-5 * want
+
+
+@pytest.mark.gpu
+def test_eval_const_off_matches_oracle(tmp_path):
+    """eval_const off: the device runs the default printed form; the oracle
+    evaluates the named constants at run time (the two forms differ by
+    ~5e-7 relative after 10 steps, oracle against oracle).  Each level within
+    1e-5 relative L2."""
+    g = simplewave_grid(grid_size=(30, 26, 28), space_order=4, ntsteps=0)
+    g.eval_const = False
+    ref0 = orun.run_regular(g, str(tmp_path / 'r0'), threads=4)['levels']['MAIN_GRID']
+    g.ntsteps.value = 10
+    ref = orun.run_regular(g, str(tmp_path / 'rn'), threads=4)['levels']['MAIN_GRID']
+    sim = _levels_sim(g, ref0)
+    sim.step(10)
+    sim.sync()
+    for lvl in range(3):
+        a, b = sim.download(lvl).astype(np.float64), ref[lvl].astype(np.float64)
+        assert np.linalg.norm(a - b) <= 1e-5 * np.linalg.norm(b), lvl
+    sim.close()
+    assert g.eval_const is False
 
 
 @pytest.mark.gpu
