@@ -110,3 +110,17 @@ def test_default_mode_executes_on_gpu_and_matches_oracle(tmp_path):
     ref = orun.run(g, str(tmp_path / 'oracle'), dump=False)['l2_fp64']
     for k, v in ref.items():
         assert abs(got[k] - v) <= 1e-4 * abs(v), (k, got[k], v)
+
+
+def test_read_mode_generates_a_file_model_program(tmp_path):
+    """``eigenwave3d.py read``: the 195^3 model whose media come from the
+    raw files RHOhomogx200, VPhomogx200 and VShomogx200 (read when the
+    program runs) is declared, solved and generated as a CUDA program."""
+    script = edited_script(tmp_path)
+    env = dict(os.environ, PYTHONPATH=PKG + os.pathsep + os.environ.get('PYTHONPATH', ''))
+    r = subprocess.run([sys.executable, str(script), 'read'], cwd=str(tmp_path), env=env,
+                       capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-3000:]
+    src = (tmp_path / 'src' / 'eigenwave3d_read.cpp').read_text()
+    for name in ('RHOhomogx200', 'VPhomogx200', 'VShomogx200', 'ofd_set_media(g_handle'):
+        assert name in src, name
