@@ -42,13 +42,13 @@ def py3_prints(text):
     return '\n'.join(out)
 
 
-def edited_script(tmp_path):
-    src = os.path.join(reference_dir(), 'tests', 'eigenwave3d.py')
+def edited_script(tmp_path, name='eigenwave3d.py'):
+    src = os.path.join(reference_dir(), 'tests', name)
     if not os.path.exists(src):
         pytest.skip('reference checkout not present')
     text = py3_prints(open(src).read())
-    compile(text, 'eigenwave3d.py', 'exec')   # valid Python 3 after the print edit alone
-    dst = tmp_path / 'eigenwave3d.py'
+    compile(text, name, 'exec')   # valid Python 3 after the print edit alone
+    dst = tmp_path / name
     dst.write_text(text)
     (tmp_path / 'src').mkdir()
     return dst
@@ -124,3 +124,42 @@ def test_read_mode_generates_a_file_model_program(tmp_path):
     src = (tmp_path / 'src' / 'eigenwave3d_read.cpp').read_text()
     for name in ('RHOhomogx200', 'VPhomogx200', 'VShomogx200', 'ofd_set_media(g_handle'):
         assert name in src, name
+
+
+@pytest.mark.skipif(not (os.path.exists('/usr/local/cuda/bin/nvcc') or
+                         subprocess.run(['which', 'nvcc'], capture_output=True).returncode == 0),
+                    reason='needs nvcc')
+def test_acoustic_script_builds_with_nvcc(tmp_path):
+    """The reference's acoustic model script, tests/simplewaveequation.py,
+    with the same print edit: ``default -c nvcc -o -p`` declares the
+    RegularGrid model, solves it and builds its CUDA program with the VTS
+    output step and profiling."""
+    script = edited_script(tmp_path, 'simplewaveequation.py')
+    env = dict(os.environ, PYTHONPATH=PKG + os.pathsep + os.environ.get('PYTHONPATH', ''))
+    r = subprocess.run([sys.executable, str(script), 'default', '-c', 'nvcc', '-o', '-p'], cwd=str(tmp_path),
+                       env=env, capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-3000:]
+    assert 'Compiled:' in r.stdout and (tmp_path / 'src' / 'regular3d').exists()
+    src = (tmp_path / 'src' / 'regular3d.cpp').read_text()
+    for s in ('ofd_regular_create', 'ofd_write_field_vts_3d(', 'profiling->g_mflops = (float)('):
+        assert s in src, s
+
+
+@pytest.mark.gpu
+def test_acoustic_script_executes_on_gpu_and_matches_oracle(tmp_path):
+    """``simplewaveequation.py default -c nvcc -x``: the 100^3, 500-step
+    model runs on the GPU through Grid.execute; its printed L2 error equals
+    the oracle's within the printed digits."""
+    script = edited_script(tmp_path, 'simplewaveequation.py')
+    env = dict(os.environ, PYTHONPATH=PKG + os.pathsep + ROOT + os.pathsep + os.environ.get('PYTHONPATH', ''))
+    r = subprocess.run([sys.executable, str(script), 'default', '-c', 'nvcc', '-x'], cwd=str(tmp_path), env=env,
+                       capture_output=True, text=True, timeout=1200)
+    assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-3000:]
+    got = {k: float(v) for k, v in _NORM.findall(r.stdout)}
+    assert 'MAIN_GRID' in got, r.stdout[-2000:]
+    from opesci.models import simplewave_grid
+    from oracle import run as orun
+    g = simplewave_grid(grid_size=(100, 100, 100), dt=0.002, tmax=1.0, space_order=4)
+    (tmp_path / 'oracle').mkdir()
+    want = orun.run_regular(g, str(tmp_path / 'oracle'))['l2_fp64']['MAIN_GRID']
+    assert abs(got['MAIN_GRID'] - want) <= 1e-4 * abs(want), (got['MAIN_GRID'], want)
